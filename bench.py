@@ -1,0 +1,324 @@
+#!/usr/bin/env python
+"""Benchmark: DOCI sigma throughput on the L=32, N=16 Hamiltonian (D = 601,080,390).
+
+One step = one sigma = H x over all D determinants, FP32 storage and
+accumulation (the sigma of the mixed-precision Davidson), on a seeded
+synthetic FCIDUMP of the benchmark's integral model.  x and sigma are 2.4 GB
+each, far larger than the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value          sigma determinants per second (whole job, Gdet/s), device-timed
+               with CUDA events on the launching stream, inputs resident in HBM.
+e2e            the same metric through the C ABI call on host buffers
+               (doci_sigma_host: H2D of x, sigma, D2H of sigma inside the call),
+               pinned host memory, wall-clock timed.
+roofline       algorithmic bytes per launch (x read 4 B + FP32 diagonal read
+               4 B + sigma write 4 B per determinant) / mean launch time,
+               against the measured HBM copy bandwidth.
+cpu_baseline   the oracle's port of the reference's race-free gather matvec
+               (FP64, all host cores) on a bounded sample of determinants.
+--impl reference  times that CPU path alone, one bounded sample per step.
+
+With torchrun (N > 1) every rank runs its own replica (the sigma has no
+cross-GPU exchange at this size); value sums the ranks' work over the slowest
+rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sigma Gdet/s; time to |ΔE|<1e-8 Ha mixed vs FP64 at L=32,N=16; p50/p99"
+UNIT = "Gdet/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--L", type=int, default=32)
+    ap.add_argument("--N", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_path(L: int, N: int, seed: int, rank: int, ws: int) -> str:
+    from doci_gb300.fcidump import write_synthetic_fcidump
+    d = os.environ.get("DOCI_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "doci_bench"))
+    os.makedirs(d, exist_ok=True)
+    p = os.path.join(d, f"synthetic_L{L}_N{N}_s{seed}.FCIDUMP")
+    if rank == 0 and not os.path.exists(p):
+        tmp = p + f".tmp{os.getpid()}"
+        write_synthetic_fcidump(tmp, L, N, seed)
+        os.replace(tmp, p)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    return p
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+            if self.uuid:
+                cmd += ["-i", self.uuid]
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(cmd, stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                c = [x.strip() for x in line.split(",")]
+                if len(c) < 9:
+                    continue
+                try:
+                    sms.append(float(c[1]))
+                    mx = float(c[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, c[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.remove(self.path)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def cpu_sample(path: str, seconds: float, seed: int = 0):
+    """Time the oracle's FP64 gather matvec (port of the reference's race-free
+    doci_full_matvec) on evenly spread determinant chunks, all host cores."""
+    import numpy as np
+
+    import oracle
+    h = oracle.Ham(path, keep_diag=False)
+    D = h.D
+    x = np.empty(D, dtype=np.float64)
+    step = 1 << 24
+    pattern = 1.0 / (1.0 + (np.arange(step) % 7))
+    for a in range(0, D, step):
+        n = min(step, D - a)
+        x[a:a + n] = pattern[:n]
+    threads = os.cpu_count() or 1
+    nchunks = 64
+
+    def run(total: int):
+        per = max(1, total // nchunks)
+        first = np.array([(c * (D - per)) // (nchunks - 1) for c in range(nchunks)], dtype=np.uint64)
+        length = np.full(nchunks, per, dtype=np.uint64)
+        rows = np.concatenate([np.arange(f, f + per, dtype=np.int64) for f in first])
+        diag = np.concatenate([h.diagonal_range(int(f), per) for f in first])
+        t0 = time.perf_counter()
+        h.gather_rows(x, first, length, diag, threads)
+        dt = time.perf_counter() - t0
+        return len(rows), dt
+
+    n0, t0 = run(64 * 2048)
+    rate = n0 / max(t0, 1e-6)
+    total = int(min(rate * seconds, D))
+    n, dt = run(max(total, 64 * 2048))
+    return {"dets": n, "seconds": dt, "rate": n / dt, "threads": threads, "D": D, "run": run}
+
+
+def main():
+    a = parse()
+    ws, rank, local = dist_env()
+    if a.impl == "reference":
+        return reference_arm(a, ws, rank)
+    import numpy as np
+    import torch
+    import doci_gb300 as dg
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    path = workload_path(a.L, a.N, a.seed, rank, ws)
+    prec = dg.FP32 if a.precision == "fp32" else dg.FP64
+    tdt = torch.float32 if prec == dg.FP32 else torch.float64
+    esize = 4 if prec == dg.FP32 else 8
+    h = dg.Hamiltonian.from_fcidump(path)
+    D = h.D
+    g = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    x = torch.randn(D, dtype=tdt, device="cuda", generator=g)
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    for _ in range(a.warmup):
+        h.sigma_device(x.data_ptr(), y.data_ptr(), prec, sptr)
+    torch.cuda.synchronize()
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(torch.cuda.current_device()).uuid)
+    except Exception:
+        pass
+    clocks = ClockSampler(uuid)
+    clocks.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps + 1)]
+    ev[0].record(stream)
+    for k in range(a.steps):
+        h.sigma_device(x.data_ptr(), y.data_ptr(), prec, sptr)
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    per_launch = [ev[k].elapsed_time(ev[k + 1]) * 1e-3 for k in range(a.steps)]
+    total = ev[0].elapsed_time(ev[a.steps]) * 1e-3
+    if ws > 1:
+        t = torch.tensor([total], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    value = D * a.steps * ws / total / 1e9
+    mean_launch = statistics.mean(per_launch)
+    bytes_alg = D * (esize + esize + esize)  # x, diagonal, sigma
+    peaks, peak_kind = measured_peaks()
+    achieved = bytes_alg / mean_launch / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"sigma_{a.precision}_L{a.L}_N{a.N}.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "bytes_per_det": 3 * esize, "mean_launch_ms": round(mean_launch * 1e3, 4)}
+    e2e = None
+    if not a.no_e2e:
+        hx = torch.randn(D, dtype=tdt, generator=torch.Generator().manual_seed(5)).pin_memory()
+        hy = torch.empty(D, dtype=tdt).pin_memory()
+        import ctypes as C
+        lib = dg.lib()
+        st = lib.doci_sigma_host(h.handle, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()), prec)
+        assert st == 0, st
+        if ws > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(a.e2e_steps):
+            st = lib.doci_sigma_host(h.handle, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()), prec)
+            assert st == 0, st
+        te = time.perf_counter() - t0
+        if ws > 1:
+            t = torch.tensor([te], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = float(t.item())
+        e2e = {"value": round(D * a.e2e_steps * ws / te / 1e9, 4), "unit": UNIT,
+               "h2d_bytes_per_step": D * esize, "d2h_bytes_per_step": D * esize,
+               "call": "doci_sigma_host (C ABI, pinned host buffers)", "steps": a.e2e_steps}
+    cpu = None
+    if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        s = cpu_sample(path, a.cpu_seconds)
+        cpu = {"value": round(s["rate"] / 1e9, 6), "unit": UNIT, "cores": s["threads"], "kind": "port",
+               "sample": f"{s['dets']} of {s['D']} determinants in 64 evenly spread chunks, FP64 gather form "
+                         f"of the reference's doci_full_matvec (oracle/doci_oracle.c), {s['seconds']:.1f} s"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": round(total / a.steps * 1e3, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == dg.FP32 else "f64",
+                "data": "synthetic (seeded FCIDUMP of the benchmark integral model)",
+                "config": {"workload": f"DOCI sigma L={a.L} N={a.N} D={D} seed={a.seed} {a.precision}",
+                           "L": a.L, "N": a.N, "D": D, "seed": a.seed, "precision": a.precision,
+                           "l2": "inputs larger than L2 (x and sigma are D*4 B = %.2f GB each)" % (D * esize / 1e9),
+                           "parallelism": f"replicas x{ws}"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": a.steps,
+                "clocks": clk, "impl": "ours"}
+        print(json.dumps(line), flush=True)
+    h.close()
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def reference_arm(a, ws, rank):
+    if rank != 0:
+        return
+    path = workload_path(a.L, a.N, a.seed, 0, 1)
+    budget = max(1.0, min(a.cpu_seconds, 150.0 / max(1, a.steps + a.warmup)))
+    s = cpu_sample(path, budget)
+    run = s["run"]
+    for _ in range(a.warmup):
+        run(s["dets"])
+    times = []
+    for _ in range(a.steps):
+        n, dt = run(s["dets"])
+        times.append(dt)
+    total = sum(times)
+    value = s["dets"] * a.steps / total / 1e9
+    line = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": 0, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(total / a.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"DOCI sigma L={a.L} N={a.N} D={s['D']} seed={a.seed} (bounded CPU sample)",
+                       "L": a.L, "N": a.N, "D": s["D"], "seed": a.seed},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": s["threads"], "kind": "port",
+                             "sample": f"{s['dets']} determinants per step in 64 evenly spread chunks, FP64 "
+                                       "gather form of the reference's doci_full_matvec (oracle/doci_oracle.c)"},
+            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,139 @@
+// addressing.cuh -- lexical determinant addressing on the device.
+//
+// The reference orders the C(L, N) determinants lexicographically by their
+// sorted occupation lists (doci.c:472-548; the last pair is advanced first)
+// and addresses them through the differenced string-graph weights Y
+// (doci.c:384-434).  The same order has a closed form: with c_0 < ... < c_{N-1}
+// the occupied orbitals,
+//     rank(T) = D - 1 - sum_e C(L-1-c_e, N-e).
+// Mirroring the orbitals (d = L-1-c) turns the sum into the combinatorial
+// number system ("colex rank") of the mirrored set M = {d_j ascending}:
+//     colex(M) = sum_j C(d_j, j+1),       rank(T) = D - 1 - colex(M).
+// In the mirrored picture the determinant's bits are brev(bits) >> (32 - L).
+//
+// Neighbour ranks.  For T' = T \ i u a (pair hop i -> a) let m_k be the
+// mirrored occupied orbital removed and q the mirrored hole filled.  With the
+// prefix sums over M of W_j = C(m_j, j+1), U_j = C(m_j, j), V_j = C(m_j, j+2)
+// and b = number of elements of M below q:
+//   q < m_k: colex(T') = [PW(b) - PV(b) + C(q, b+1)] + [PV(k) + R - PW(k+1)]
+//   q > m_k: colex(T') = [PU(b) + R - PW(b) + C(q, b)] + [PW(k) - PU(k+1)]
+// where R = colex(M).  The first bracket depends only on the hole (E1/E2
+// below), the second only on the removed element (c1/c2): every one of the
+// N(L-N) neighbour ranks costs one compare and one add, the job the
+// reference's incremental Y-walk does in prev_bitstring (doci.c:851-978).
+#pragma once
+
+#include <cstdint>
+
+namespace doci {
+namespace dev {
+
+#ifdef __CUDA_ARCH__
+#define DOCI_HD __host__ __device__ __forceinline__
+__device__ __forceinline__ int ffs32(uint32_t v) { return __ffs(static_cast<int>(v)); }
+#else
+#define DOCI_HD __host__ __device__ inline
+inline int ffs32(uint32_t v) { return __builtin_ffs(static_cast<int>(v)); }
+#endif
+
+__host__ __device__ __forceinline__ uint32_t low_mask(int L) {
+  return L >= 32 ? 0xffffffffu : ((1u << L) - 1u);
+}
+
+// colex unrank: the N-subset of {0..L-1} (mirrored orbitals) with colex rank R
+template <int BC>
+DOCI_HD uint32_t colex_unrank(uint32_t R, int L, int N, const uint32_t *binom) {
+  uint32_t M = 0;
+  int d = L - 1;
+  for (int j = N; j >= 1; --j) {
+    while (binom[d * BC + j] > R) --d;
+    R -= binom[d * BC + j];
+    M |= 1u << d;
+    --d;
+  }
+  return M;
+}
+
+template <int BC>
+DOCI_HD uint32_t colex_rank(uint32_t M, const uint32_t *binom) {
+  uint32_t s = 0;
+  int j = 0;
+  while (M) {
+    const int d = ffs32(M) - 1;
+    M &= M - 1;
+    s += binom[d * BC + j + 1];
+    ++j;
+  }
+  return s;
+}
+
+DOCI_HD uint32_t mirror_bits(uint32_t bits, int L) {
+#ifdef __CUDA_ARCH__
+  return __brev(bits) >> (32 - L);
+#else
+  uint32_t r = 0;
+  for (int o = 0; o < L; ++o)
+    if (bits >> o & 1u) r |= 1u << (L - 1 - o);
+  return r;
+#endif
+}
+
+// Neighbour enumeration of one determinant (rank r, colex R = D-1-r, mirrored
+// occupation M).  Precompute() fills the per-hole terms; then for every
+// occupied element k (ascending mirrored orbital m) and hole h (ascending q),
+// visit(m, q, rank(T')) is called.  Shared by the sigma kernels and by the
+// host-side index check.
+template <int NH, int BC>
+struct Neighbours {
+  uint32_t E1[NH], E2[NH];
+  int Q[NH];
+  DOCI_HD void precompute(uint32_t M, uint32_t R, int L, int nh, const uint32_t *B) {
+    uint32_t holes = ~M & low_mask(L), mrem = M, PW = 0, PU = 0, PV = 0;
+    int j = 0;
+#pragma unroll
+    for (int h = 0; h < NH; ++h) {
+      if (h < nh) {
+        const int q = ffs32(holes) - 1;
+        holes &= holes - 1;
+        while (mrem && (ffs32(mrem) - 1) < q) {
+          const int m = ffs32(mrem) - 1;
+          mrem &= mrem - 1;
+          PW += B[m * BC + j + 1];
+          PU += B[m * BC + j];
+          PV += B[m * BC + j + 2];
+          ++j;
+        }
+        // j == q - h elements of M lie below q
+        E1[h] = PW - PV + B[q * BC + j + 1];
+        E2[h] = PU + R - PW + B[q * BC + j];
+        Q[h] = q;
+      } else {
+        E1[h] = E2[h] = 0;
+        Q[h] = 0;
+      }
+    }
+  }
+  template <typename F>
+  DOCI_HD void visit(uint32_t M, uint32_t R, uint32_t Dm1, int N, int nh, const uint32_t *B, F &&f) const {
+    uint32_t mrem = M, PW = 0, PU = 0, PV = 0;
+    for (int k = 0; k < N; ++k) {
+      const int m = ffs32(mrem) - 1;
+      mrem &= mrem - 1;
+      const uint32_t W = B[m * BC + k + 1], U = B[m * BC + k], V = B[m * BC + k + 2];
+      // rank(T') = D-1 - (E + c)
+      const uint32_t base1 = Dm1 - (PV + R - (PW + W));
+      const uint32_t base2 = Dm1 - (PW - (PU + U));
+      f.begin(m);
+#pragma unroll
+      for (int h = 0; h < NH; ++h) {
+        if (h < nh) f.hop(m, Q[h], Q[h] < m ? base1 - E1[h] : base2 - E2[h]);
+      }
+      PW += W;
+      PU += U;
+      PV += V;
+    }
+  }
+};
+
+}  // namespace dev
+}  // namespace doci

@@ -1,0 +1,139 @@
+// ham.cu -- device Hamiltonian: integral tables, addressing tables, diagonal.
+//
+// Setup of doci.c:69-134 (fill_doci_data) on the GPU: the lexical string-graph
+// tables (doci.c:384-470) become one binomial table, the D-sized bitstring
+// table (doci.c:472-548) is never built (kernels unrank on the fly), and the
+// diagonal (doci.c:550-628) is computed by a kernel into HBM, in FP64 and as
+// an FP32 copy for the FP32 sigma.
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <cstring>
+
+#include "internal.h"
+
+namespace doci {
+
+static thread_local char g_last_cuda_error[256];
+
+int cuda_status(cudaError_t e, const char *what) {
+  std::snprintf(g_last_cuda_error, sizeof g_last_cuda_error, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();  // clear the sticky-free allocation error
+    return DOCI_ERR_OUT_OF_MEMORY;
+  }
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return DOCI_ERR_NO_DEVICE;
+  return DOCI_ERR_CUDA;
+}
+
+const char *last_cuda_error() { return g_last_cuda_error; }
+
+int device_sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+  }
+  return sms;
+}
+
+void ham_release(doci_ham *h) {
+  if (!h) return;
+  cudaFree(h->d_binom);
+  cudaFree(h->d_Kmir64);
+  cudaFree(h->d_Kmir32);
+  cudaFree(h->d_tab64);
+  cudaFree(h->d_diag);
+  cudaFree(h->d_diag32);
+  cudaFree(h->d_stage_x);
+  cudaFree(h->d_stage_y);
+  if (h->h_diag) cudaFreeHost(h->h_diag);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  h->d_binom = nullptr;
+  h->d_Kmir64 = h->d_tab64 = h->d_diag = nullptr;
+  h->d_Kmir32 = h->d_diag32 = nullptr;
+  h->d_stage_x = h->d_stage_y = nullptr;
+  h->h_diag = nullptr;
+  h->stream = nullptr;
+}
+
+int ham_stage(doci_ham *h, size_t bytes) {
+  if (h->stage_bytes >= bytes) return DOCI_OK;
+  cudaFree(h->d_stage_x);
+  cudaFree(h->d_stage_y);
+  h->d_stage_x = h->d_stage_y = nullptr;
+  h->stage_bytes = 0;
+  DOCI_CUDA(cudaMalloc(&h->d_stage_x, bytes));
+  DOCI_CUDA(cudaMalloc(&h->d_stage_y, bytes));
+  h->stage_bytes = bytes;
+  return DOCI_OK;
+}
+
+// `in` holds the raw integrals (as read from an FCIDUMP); the transform is
+// applied to a copy.
+int ham_build(doci_ham *h, const Integrals &in) {
+  const int L = in.L;
+  if (L < 1) return DOCI_ERR_INVALID;
+  if (L > kMaxOrbitals) return DOCI_ERR_TOO_MANY_ORBITALS;
+  if (in.Na != in.Nb) return DOCI_ERR_NALPHA_NBETA;
+  if (in.Na < 0 || in.Na > L) return DOCI_ERR_INVALID;
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count < 1) {
+    cudaGetLastError();
+    return DOCI_ERR_NO_DEVICE;
+  }
+  std::vector<double> one(in.one), two(in.two);
+  transform_integrals(one.data(), two.data(), L);
+  const size_t n = L, n2 = n * n, n3 = n2 * n;
+  h->L = L;
+  h->N = in.Na;
+  h->nh = L - in.Na;
+  h->core = in.core;
+  h->D = combination(static_cast<unsigned>(in.Na), static_cast<unsigned>(L));
+  h->h2.assign(n, 0);
+  h->J2.assign(n2, 0);
+  h->Kx.assign(n2, 0);
+  h->Kp.assign(n2, 0);
+  for (size_t i = 0; i < n; ++i) {
+    h->h2[i] = 2 * one[i * (n + 1)];
+    for (size_t j = 0; j < n; ++j) {
+      h->J2[i * n + j] = 2 * two[i + i * n + j * n2 + j * n3];  // 2 (ii|jj)
+      h->Kx[i * n + j] = two[i + j * n + j * n2 + i * n3];      // (ij|ji)
+      h->Kp[i * n + j] = i == j ? 0.0 : two[i + j * n + i * n2 + j * n3];  // (ij|ij)
+    }
+  }
+  cudaGetDevice(&h->device);
+  DOCI_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+
+  std::vector<uint32_t> binom(kBinomRows * kBinomCols);
+  fill_binom_table(binom.data());
+  std::vector<double> kmir(32 * 32, 0.0);
+  std::vector<float> kmir32(32 * 32, 0.0f);
+  for (int m = 0; m < L; ++m)
+    for (int q = 0; q < L; ++q) {
+      kmir[m * 32 + q] = h->Kp[(L - 1 - m) * n + (L - 1 - q)];
+      kmir32[m * 32 + q] = static_cast<float>(kmir[m * 32 + q]);
+    }
+  std::vector<double> tab(n + 2 * n2);
+  std::memcpy(tab.data(), h->h2.data(), n * sizeof(double));
+  std::memcpy(tab.data() + n, h->J2.data(), n2 * sizeof(double));
+  std::memcpy(tab.data() + n + n2, h->Kx.data(), n2 * sizeof(double));
+
+  DOCI_CUDA(cudaMalloc(&h->d_binom, binom.size() * sizeof(uint32_t)));
+  DOCI_CUDA(cudaMalloc(&h->d_Kmir64, 32 * 32 * sizeof(double)));
+  DOCI_CUDA(cudaMalloc(&h->d_Kmir32, 32 * 32 * sizeof(float)));
+  DOCI_CUDA(cudaMalloc(&h->d_tab64, tab.size() * sizeof(double)));
+  DOCI_CUDA(cudaMalloc(&h->d_diag, static_cast<size_t>(h->D) * sizeof(double)));
+  DOCI_CUDA(cudaMalloc(&h->d_diag32, static_cast<size_t>(h->D) * sizeof(float)));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_binom, binom.data(), binom.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_Kmir64, kmir.data(), kmir.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_Kmir32, kmir32.data(), kmir32.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_tab64, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int st = launch_diagonal(h, h->stream);
+  if (st) return st;
+  DOCI_CUDA(cudaStreamSynchronize(h->stream));
+  return DOCI_OK;
+}
+
+}  // namespace doci

@@ -1,0 +1,96 @@
+// internal.h -- shared definitions of libdoci_gb300 (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/doci_gb300.h"
+
+namespace doci {
+
+constexpr int kMaxOrbitals = 32;
+// binomial table C(n, k) for n = 0..32 and k = 0..34 (k up to N + 2 is read
+// by the neighbour-rank prefix sums)
+constexpr int kBinomRows = 33;
+constexpr int kBinomCols = 35;
+
+// Integrals after the reference's transform (doci.c:630-665), reduced to the
+// L x L tables the DOCI Hamiltonian needs.
+struct Integrals {
+  int L = 0, Na = 0, Nb = 0;
+  double core = 0;
+  std::vector<double> one;  // h' (L*L), after the transform
+  std::vector<double> two;  // (ij|kl) (L^4), after the transform
+};
+
+// FCIDUMP reader restating read_fcidump.c:18-82; returns a doci_status and
+// the offending line number on a format error.
+int read_fcidump_file(const char *path, Integrals *out, int *bad_line);
+// doci.c:630-665 (in place)
+void transform_integrals(double *one, double *two, int L);
+// doci.c:687-701
+uint32_t combination(unsigned n, unsigned m);
+uint64_t binom64(unsigned n, unsigned k);
+void fill_binom_table(uint32_t *t);  // kBinomRows x kBinomCols
+
+// cached device properties
+int device_sm_count();
+
+// CUDA error plumbing: every CUDA call goes through check(); the first
+// failure is remembered per thread for doci_status_string.
+int cuda_status(cudaError_t e, const char *what);
+#define DOCI_CUDA(call)                                       \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return ::doci::cuda_status(_e, #call); \
+  } while (0)
+
+}  // namespace doci
+
+// The opaque handle of the C ABI.
+struct doci_ham {
+  int L = 0, N = 0;
+  uint32_t D = 0;
+  int nh = 0;  // holes per determinant, L - N
+  double core = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+
+  // host tables (L x L, row-major by first orbital)
+  std::vector<double> h2;   // 2 h'_ii
+  std::vector<double> J2;   // 2 (ii|jj)
+  std::vector<double> Kx;   // (ij|ji)
+  std::vector<double> Kp;   // (ia|ia), zero diagonal (Viikk, doci.c:667-683)
+
+  // device tables
+  uint32_t *d_binom = nullptr;   // kBinomRows x kBinomCols
+  double *d_Kmir64 = nullptr;    // 32 x 32, mirrored orbitals: [m][q] = K[L-1-m][L-1-q]
+  float *d_Kmir32 = nullptr;
+  double *d_tab64 = nullptr;     // h2 | J2 | Kx for the diagonal kernel
+  double *d_diag = nullptr;      // D, FP64 diagonal
+  float *d_diag32 = nullptr;     // D, FP32 copy
+
+  // host diagonal for doci_get_diagonal (lazy)
+  double *h_diag = nullptr;
+  // device staging for the host-buffer entry points (lazy)
+  void *d_stage_x = nullptr, *d_stage_y = nullptr;
+  size_t stage_bytes = 0;
+  // the reference-compatible handle prints its banner once
+  bool from_fill = false;
+};
+
+namespace doci {
+// ham.cu
+int ham_build(doci_ham *h, const Integrals &in);
+void ham_release(doci_ham *h);
+int ham_stage(doci_ham *h, size_t bytes);
+// sigma.cu
+int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t s);
+int launch_bitstrings(const doci_ham *h, int64_t first, int64_t count, uint32_t *out, cudaStream_t s);
+int launch_ranks(const doci_ham *h, const uint32_t *bits, int64_t count, int64_t *out, cudaStream_t s);
+int launch_diagonal(doci_ham *h, cudaStream_t s);
+}  // namespace doci

@@ -1,0 +1,64 @@
+// solvers.h -- device-resident Davidson and RQ-CG drivers (solvers.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <vector>
+
+#include "internal.h"
+
+namespace doci {
+
+// The matvec a solver calls once per iteration: the device sigma of `ham`
+// (in the solver's storage precision), or a host function on FP64 buffers.
+struct MatvecOp {
+  doci_ham *ham = nullptr;
+  void (*host_fn)(double *, double *, void *) = nullptr;
+  void *host_dat = nullptr;
+  size_t n = 0;
+  std::vector<double> hx, hy;
+  double sigma_seconds = 0;
+  bool events_on = false;
+  cudaEvent_t ev0{}, ev1{};
+  int apply(const void *d_x, void *d_y, int precision, cudaStream_t st);
+  void enable_timing();
+  ~MatvecOp();
+};
+
+struct DavidsonArgs {
+  int max_vectors = 30, keep = 2, max_its = 200;
+  double tol = 1e-8;
+  int print_table = 0;    // the -DDAVIDIT table of davidson.c:47-112
+  int print_summary = 0;  // "** DAVIDSON ITERATIONS" (davidson.c:114)
+  int stall_window = 0;   // > 0: stop when the residual stops halving (FP32 phase)
+  double *trace = nullptr;  // optional per-iteration (residual, energy)
+  int trace_len = 0;
+};
+
+struct DavidsonOut {
+  double energy = 0, residual = 0, seconds = 0;
+  int iterations = 0, converged = 0, return_code = 0;
+};
+
+struct CgArgs {
+  int max_its = 200;
+  double tol = 1e-8;
+  int print = 1;  // CG.c prints its table unconditionally
+  double *trace = nullptr;
+  int trace_len = 0;
+};
+
+struct CgOut {
+  double energy = 0, normq = 0, normq_g = 0, seconds = 0;
+  int iterations = 0, converged = 0, return_code = 0;
+};
+
+template <typename S>
+int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const DavidsonArgs &a, cudaStream_t st,
+                 DavidsonOut *out, double *d_x_out);
+
+int ray_q_run(MatvecOp &op, size_t D, const double *d_diag_or_null, double *d_x, const CgArgs &a, cudaStream_t st,
+              CgOut *out);
+
+}  // namespace doci

@@ -1,0 +1,528 @@
+// vec.cu -- the Davidson / RQ-CG vector layer on the device.
+//
+// The reference runs these steps as BLAS calls on host arrays
+// (davidson.c:133-255, CG.c:74-127).  Here they are fused passes over HBM:
+//  * residual pass: x = V y, r = VA y - theta x, ||r||, the preconditioned
+//    t = r / |diag - theta| (davidson.c:195-227) and the first Gram-Schmidt
+//    projections V^T t, all in one read of V and VA;
+//  * Gram-Schmidt: classical GS applied twice (projection pass, update +
+//    second projection pass, final update + normalisation), replacing the
+//    single modified-GS sweep of davidson.c:139-146;
+//  * subspace column V^T (H v_m) (davidson.c:178-193) as a multi-dot;
+//  * deflation V <- V Y[:, :keep] in place (davidson.c:229-255);
+//  * RQ-CG: the 2x2 Gram blocks of CG.c:102-103 in one pass, and the x/Ax/g
+//    updates of CG.c:106-126 in one pass.
+// Storage is double (FP64 mode) or float (FP32 basis of the mixed mode);
+// every product is accumulated in FP64.  Reductions are two-stage
+// (per-block partials, then one block summing them in a fixed order), so
+// results do not depend on timing.
+#include <cuda_runtime.h>
+
+#include "internal.h"
+#include "vec.h"
+
+namespace doci {
+namespace {
+
+constexpr int kT = 256;
+constexpr int kMaxK = 34;  // outputs of one reduction pass
+
+int grid_blocks() { return device_sm_count() * 2; }
+
+template <int K>
+__device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, double *partials) {
+  __shared__ double red[kT / 32][kMaxK];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (k < nk) {
+      double v = acc[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][k] = v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nk) {
+    double s = 0;
+    for (int w = 0; w < kT / 32; ++w) s += red[w][threadIdx.x];
+    partials[static_cast<size_t>(blockIdx.x) * nk + threadIdx.x] = s;
+  }
+}
+
+// out[k] = sum_b partials[b][k]; fixed order
+__global__ void reduce_partials_kernel(const double *__restrict__ partials, int nblocks, int nk,
+                                       double *__restrict__ out) {
+  __shared__ double red[kT];
+  for (int k = 0; k < nk; ++k) {
+    double s = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[static_cast<size_t>(b) * nk + k];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = red[0];
+    __syncthreads();
+  }
+}
+
+// partials of V_i . w for i < m
+template <typename S, int K>
+__global__ void __launch_bounds__(kT)
+multidot_kernel(const S *__restrict__ V, size_t ld, int m, const S *__restrict__ w, size_t n,
+                double *__restrict__ partials) {
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0;
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    const double wj = static_cast<double>(w[j]);
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < m) acc[k] += static_cast<double>(V[k * ld + j]) * wj;
+  }
+  block_reduce_store<K>(acc, m, partials);
+}
+
+// Residual pass.  Outputs (per block): [0] ||r||^2, [1] ||t||^2, [2..2+m) V_i . t
+template <typename S, int K>
+__global__ void __launch_bounds__(kT)
+residual_kernel(const S *__restrict__ V, const S *__restrict__ VA, size_t ld, int m,
+                const double *__restrict__ y, double theta, const double *__restrict__ diag, size_t n,
+                S *__restrict__ t, double *__restrict__ x_out, double *__restrict__ partials) {
+  __shared__ double ys[K];
+  if (threadIdx.x < K) ys[threadIdx.x] = threadIdx.x < m ? y[threadIdx.x] : 0.0;
+  __syncthreads();
+  double acc[K + 2];
+#pragma unroll
+  for (int k = 0; k < K + 2; ++k) acc[k] = 0;
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    double v[K];
+    double xv = 0, av = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (k < m) {
+        v[k] = static_cast<double>(V[k * ld + j]);
+        xv += v[k] * ys[k];
+        av += static_cast<double>(VA[k * ld + j]) * ys[k];
+      }
+    }
+    const double r = av - theta * xv;
+    acc[0] += r * r;
+    if (x_out) x_out[j] = xv;
+    const double d = fabs(diag[j] - theta);
+    const S ts = static_cast<S>(d > 1e-12 ? r / d : r / 1e-12);  // davidson.c:214-227
+    t[j] = ts;
+    const double td = static_cast<double>(ts);
+    acc[1] += td * td;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < m) acc[2 + k] += v[k] * td;
+  }
+  block_reduce_store<K + 2>(acc, m + 2, partials);
+}
+
+// t <- t - sum_i c_i V_i; partials: [0] ||t||^2, [1..1+m) V_i . t
+template <typename S, int K>
+__global__ void __launch_bounds__(kT)
+gs_update_kernel(const S *__restrict__ V, size_t ld, int m, const double *__restrict__ c, size_t n,
+                 S *__restrict__ t, double *__restrict__ partials) {
+  __shared__ double cs[K];
+  if (threadIdx.x < K) cs[threadIdx.x] = threadIdx.x < m ? c[threadIdx.x] : 0.0;
+  __syncthreads();
+  double acc[K + 1];
+#pragma unroll
+  for (int k = 0; k < K + 1; ++k) acc[k] = 0;
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    double v[K];
+    double tv = static_cast<double>(t[j]);
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < m) {
+        v[k] = static_cast<double>(V[k * ld + j]);
+        tv -= v[k] * cs[k];
+      }
+    const S ts = static_cast<S>(tv);
+    t[j] = ts;
+    const double td = static_cast<double>(ts);
+    acc[0] += td * td;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < m) acc[1 + k] += v[k] * td;
+  }
+  block_reduce_store<K + 1>(acc, m + 1, partials);
+}
+
+// out = (t - sum_i c_i V_i) * scale; partials: [0] ||out||^2
+template <typename S, int K>
+__global__ void __launch_bounds__(kT)
+gs_finish_kernel(const S *__restrict__ V, size_t ld, int m, const double *__restrict__ c, double scale,
+                 size_t n, const S *__restrict__ t, S *__restrict__ out, double *__restrict__ partials) {
+  __shared__ double cs[K];
+  if (threadIdx.x < K) cs[threadIdx.x] = threadIdx.x < m ? c[threadIdx.x] : 0.0;
+  __syncthreads();
+  double acc[1] = {0};
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    double tv = static_cast<double>(t[j]);
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < m) tv -= static_cast<double>(V[k * ld + j]) * cs[k];
+    const S o = static_cast<S>(tv * scale);
+    out[j] = o;
+    acc[0] += static_cast<double>(o) * static_cast<double>(o);
+  }
+  block_reduce_store<1>(acc, 1, partials);
+}
+
+// V[:, c] <- sum_k V[:, k] Y[k, c] for c < keep, in place (each element's
+// row is read completely before it is written).
+template <typename S, int K>
+__global__ void __launch_bounds__(kT)
+deflate_kernel(S *__restrict__ V, size_t ld, int mv, int keep, const double *__restrict__ Y, int ldy, size_t n) {
+  __shared__ double Ys[K * K];
+  for (int i = threadIdx.x; i < mv * keep; i += blockDim.x) Ys[i] = Y[(i / mv) * ldy + (i % mv)];
+  __syncthreads();
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < mv) v[k] = static_cast<double>(V[k * ld + j]);
+    for (int c = 0; c < keep; ++c) {
+      double s = 0;
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (k < mv) s += v[k] * Ys[c * mv + k];
+      V[c * ld + j] = static_cast<S>(s);
+    }
+  }
+}
+
+// x = V y (FP64 output)
+template <typename S, int K>
+__global__ void __launch_bounds__(kT)
+combine_kernel(const S *__restrict__ V, size_t ld, int m, const double *__restrict__ y, size_t n,
+               double *__restrict__ x) {
+  __shared__ double ys[K];
+  if (threadIdx.x < K) ys[threadIdx.x] = threadIdx.x < m ? y[threadIdx.x] : 0.0;
+  __syncthreads();
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < m) s += static_cast<double>(V[k * ld + j]) * ys[k];
+    x[j] = s;
+  }
+}
+
+template <typename A, typename B>
+__global__ void convert_kernel(const A *__restrict__ a, B *__restrict__ b, size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    b[j] = static_cast<B>(a[j]);
+}
+
+template <typename S>
+__global__ void scale_kernel(const S *__restrict__ a, double s, S *__restrict__ b, size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    b[j] = static_cast<S>(static_cast<double>(a[j]) * s);
+}
+
+// ---- RQ-CG (CG.c) --------------------------------------------------------
+// partials: x.Ax, p.Ax, x.Ap, p.Ap, x.x, x.p, p.p
+__global__ void __launch_bounds__(kT)
+cg_gram_kernel(const double *__restrict__ x, const double *__restrict__ p, const double *__restrict__ Ax,
+               const double *__restrict__ Ap, size_t n, double *__restrict__ partials) {
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    const double xv = x[j], pv = p[j], ax = Ax[j], ap = Ap[j];
+    acc[0] += xv * ax;
+    acc[1] += pv * ax;
+    acc[2] += xv * ap;
+    acc[3] += pv * ap;
+    acc[4] += xv * xv;
+    acc[5] += xv * pv;
+    acc[6] += pv * pv;
+  }
+  block_reduce_store<7>(acc, 7, partials);
+}
+
+// x <- a x + b p, Ax <- a Ax + b Ap (skipped when first), g = 2 (Ax - rho x);
+// partials: [0] g.g, then g <- g * pinv, [1] g.g
+__global__ void __launch_bounds__(kT)
+cg_update_kernel(double a, double b, int first, double rho, double *__restrict__ x, const double *__restrict__ p,
+                 double *__restrict__ Ax, const double *__restrict__ Ap, double *__restrict__ g,
+                 const double *__restrict__ pinv, size_t n, double *__restrict__ partials) {
+  double acc[2] = {0, 0};
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    double xv = x[j], ax = Ax[j];
+    if (!first) {
+      xv = a * xv + b * p[j];
+      ax = a * ax + b * Ap[j];
+      x[j] = xv;
+      Ax[j] = ax;
+    }
+    double gv = 2 * (ax - rho * xv);
+    acc[0] += gv * gv;
+    if (pinv) gv *= pinv[j];
+    g[j] = gv;
+    acc[1] += gv * gv;
+  }
+  block_reduce_store<2>(acc, 2, partials);
+}
+
+// p <- beta p - g (first: p = -g)
+__global__ void cg_direction_kernel(double beta, int first, double *__restrict__ p, const double *__restrict__ g,
+                                    size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    p[j] = first ? -g[j] : beta * p[j] - g[j];
+}
+
+// CG.c:57-63
+__global__ void precond_inverse_kernel(const double *__restrict__ diag, double *__restrict__ pinv, size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    pinv[j] = fabs(diag[j]) > 1e-12 ? 1.0 / diag[j] : 1.0 / 1e-12;
+}
+
+
+// ---- start vectors (executable.c:270-299) --------------------------------
+// first index of the minimum (the reference scans with a strict <)
+__global__ void argmin_partial_kernel(const double *__restrict__ d, size_t n, double *__restrict__ pv,
+                                      int64_t *__restrict__ pi) {
+  __shared__ double sv[kT];
+  __shared__ int64_t si[kT];
+  double best = INFINITY;
+  int64_t bi = -1;
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    const double v = d[j];
+    if (v < best) {
+      best = v;
+      bi = static_cast<int64_t>(j);
+    }
+  }
+  sv[threadIdx.x] = best;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      const double ov = sv[threadIdx.x + w];
+      const int64_t oi = si[threadIdx.x + w];
+      if (oi >= 0 && (si[threadIdx.x] < 0 || ov < sv[threadIdx.x] || (ov == sv[threadIdx.x] && oi < si[threadIdx.x]))) {
+        sv[threadIdx.x] = ov;
+        si[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    pv[blockIdx.x] = sv[0];
+    pi[blockIdx.x] = si[0];
+  }
+}
+
+__global__ void argmin_final_kernel(const double *__restrict__ pv, const int64_t *__restrict__ pi, int nb,
+                                    int64_t *__restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double best = INFINITY;
+  int64_t bi = 0;
+  bool any = false;
+  for (int b = 0; b < nb; ++b) {
+    if (pi[b] < 0) continue;
+    if (!any || pv[b] < best || (pv[b] == best && pi[b] < bi)) {
+      best = pv[b];
+      bi = pi[b];
+      any = true;
+    }
+  }
+  *out = bi;
+}
+
+__global__ void set_unit_kernel(double *__restrict__ t, size_t n, const int64_t *__restrict__ idx) {
+  const int64_t k = *idx;
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    t[j] = static_cast<int64_t>(j) == k ? 1.0 : 0.0;
+}
+
+// positive uniform numbers in (0, 1] from a counter-based hash (splitmix64)
+__global__ void fill_random_kernel(double *__restrict__ t, size_t n, uint64_t seed) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    uint64_t z = seed * 0x9E3779B97F4A7C15ull + j + 1;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    t[j] = (static_cast<double>(z >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+  }
+}
+
+template <typename S, template <typename, int> class Kern, typename... Args>
+int dispatch_k(int m, cudaStream_t st, Args... args) {
+  const int g = grid_blocks();
+  if (m <= 8) Kern<S, 8>::run(g, st, args...);
+  else if (m <= 16) Kern<S, 16>::run(g, st, args...);
+  else Kern<S, 32>::run(g, st, args...);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+template <typename S, int K>
+struct MultidotL {
+  static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const S *w, size_t n, double *p) {
+    multidot_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, w, n, p);
+  }
+};
+template <typename S, int K>
+struct ResidualL {
+  static void run(int g, cudaStream_t st, const S *V, const S *VA, size_t ld, int m, const double *y, double th,
+                  const double *diag, size_t n, S *t, double *x, double *p) {
+    residual_kernel<S, K><<<g, kT, 0, st>>>(V, VA, ld, m, y, th, diag, n, t, x, p);
+  }
+};
+template <typename S, int K>
+struct GsUpdateL {
+  static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *p) {
+    gs_update_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, c, n, t, p);
+  }
+};
+template <typename S, int K>
+struct GsFinishL {
+  static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, double sc, size_t n,
+                  const S *t, S *out, double *p) {
+    gs_finish_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, c, sc, n, t, out, p);
+  }
+};
+template <typename S, int K>
+struct DeflateL {
+  static void run(int g, cudaStream_t st, S *V, size_t ld, int mv, int keep, const double *Y, int ldy, size_t n) {
+    deflate_kernel<S, K><<<g, kT, 0, st>>>(V, ld, mv, keep, Y, ldy, n);
+  }
+};
+template <typename S, int K>
+struct CombineL {
+  static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *y, size_t n, double *x) {
+    combine_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, y, n, x);
+  }
+};
+
+}  // namespace
+
+int vec_partials_capacity() { return grid_blocks() * kMaxK; }
+
+int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st) {
+  reduce_partials_kernel<<<1, kT, 0, st>>>(partials, grid_blocks(), nk, out);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+template <typename S>
+int vec_multidot(const S *V, size_t ld, int m, const S *w, size_t n, double *partials, cudaStream_t st) {
+  if (m < 1 || m > 32) return DOCI_ERR_INVALID;
+  return dispatch_k<S, MultidotL>(m, st, V, ld, m, w, n, partials);
+}
+template <typename S>
+int vec_residual(const S *V, const S *VA, size_t ld, int m, const double *y, double theta, const double *diag,
+                 size_t n, S *t, double *x, double *partials, cudaStream_t st) {
+  if (m < 1 || m > 32) return DOCI_ERR_INVALID;
+  return dispatch_k<S, ResidualL>(m, st, V, VA, ld, m, y, theta, diag, n, t, x, partials);
+}
+template <typename S>
+int vec_gs_update(const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *partials, cudaStream_t st) {
+  if (m < 1 || m > 32) return DOCI_ERR_INVALID;
+  return dispatch_k<S, GsUpdateL>(m, st, V, ld, m, c, n, t, partials);
+}
+template <typename S>
+int vec_gs_finish(const S *V, size_t ld, int m, const double *c, double scale, size_t n, const S *t, S *out,
+                  double *partials, cudaStream_t st) {
+  if (m < 0 || m > 32) return DOCI_ERR_INVALID;
+  if (m == 0) {
+    scale_kernel<S><<<grid_blocks(), kT, 0, st>>>(t, scale, out, n);
+    DOCI_CUDA(cudaGetLastError());
+    return DOCI_OK;
+  }
+  return dispatch_k<S, GsFinishL>(m, st, V, ld, m, c, scale, n, t, out, partials);
+}
+template <typename S>
+int vec_deflate(S *V, size_t ld, int mv, int keep, const double *Y, int ldy, size_t n, cudaStream_t st) {
+  if (mv < 1 || mv > 32 || keep < 1 || keep > mv) return DOCI_ERR_INVALID;
+  return dispatch_k<S, DeflateL>(mv, st, V, ld, mv, keep, Y, ldy, n);
+}
+template <typename S>
+int vec_combine(const S *V, size_t ld, int m, const double *y, size_t n, double *x, cudaStream_t st) {
+  if (m < 1 || m > 32) return DOCI_ERR_INVALID;
+  return dispatch_k<S, CombineL>(m, st, V, ld, m, y, n, x);
+}
+template <typename A, typename B>
+int vec_convert(const A *a, B *b, size_t n, cudaStream_t st) {
+  convert_kernel<A, B><<<grid_blocks(), kT, 0, st>>>(a, b, n);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+
+int vec_argmin(const double *d, size_t n, int64_t *idx, cudaStream_t st) {
+  const int g = grid_blocks();
+  double *pv = nullptr;
+  DOCI_CUDA(cudaMallocAsync(&pv, (sizeof(double) + sizeof(int64_t)) * g + sizeof(int64_t), st));
+  int64_t *pi = reinterpret_cast<int64_t *>(pv + g), *out = pi + g;
+  argmin_partial_kernel<<<g, kT, 0, st>>>(d, n, pv, pi);
+  argmin_final_kernel<<<1, 32, 0, st>>>(pv, pi, g, out);
+  DOCI_CUDA(cudaGetLastError());
+  DOCI_CUDA(cudaMemcpyAsync(idx, out, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  DOCI_CUDA(cudaStreamSynchronize(st));
+  DOCI_CUDA(cudaFreeAsync(pv, st));
+  return DOCI_OK;
+}
+
+int vec_set_unit(double *t, size_t n, int64_t idx, cudaStream_t st) {
+  int64_t *d_idx = nullptr;
+  DOCI_CUDA(cudaMallocAsync(&d_idx, sizeof(int64_t), st));
+  DOCI_CUDA(cudaMemcpyAsync(d_idx, &idx, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+  set_unit_kernel<<<grid_blocks(), kT, 0, st>>>(t, n, d_idx);
+  DOCI_CUDA(cudaGetLastError());
+  DOCI_CUDA(cudaFreeAsync(d_idx, st));
+  DOCI_CUDA(cudaStreamSynchronize(st));
+  return DOCI_OK;
+}
+
+int vec_fill_random(double *t, size_t n, uint64_t seed, cudaStream_t st) {
+  fill_random_kernel<<<grid_blocks(), kT, 0, st>>>(t, n, seed);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+int cg_gram(const double *x, const double *p, const double *Ax, const double *Ap, size_t n, double *partials,
+            cudaStream_t st) {
+  cg_gram_kernel<<<grid_blocks(), kT, 0, st>>>(x, p, Ax, Ap, n, partials);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+int cg_update(double a, double b, int first, double rho, double *x, const double *p, double *Ax, const double *Ap,
+              double *g, const double *pinv, size_t n, double *partials, cudaStream_t st) {
+  cg_update_kernel<<<grid_blocks(), kT, 0, st>>>(a, b, first, rho, x, p, Ax, Ap, g, pinv, n, partials);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+int cg_direction(double beta, int first, double *p, const double *g, size_t n, cudaStream_t st) {
+  cg_direction_kernel<<<grid_blocks(), kT, 0, st>>>(beta, first, p, g, n);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+int precond_inverse(const double *diag, double *pinv, size_t n, cudaStream_t st) {
+  precond_inverse_kernel<<<grid_blocks(), kT, 0, st>>>(diag, pinv, n);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+#define DOCI_VEC_INST(S)                                                                                   \
+  template int vec_multidot<S>(const S *, size_t, int, const S *, size_t, double *, cudaStream_t);          \
+  template int vec_residual<S>(const S *, const S *, size_t, int, const double *, double, const double *,   \
+                               size_t, S *, double *, double *, cudaStream_t);                              \
+  template int vec_gs_update<S>(const S *, size_t, int, const double *, size_t, S *, double *, cudaStream_t); \
+  template int vec_gs_finish<S>(const S *, size_t, int, const double *, double, size_t, const S *, S *,      \
+                                double *, cudaStream_t);                                                    \
+  template int vec_deflate<S>(S *, size_t, int, int, const double *, int, size_t, cudaStream_t);            \
+  template int vec_combine<S>(const S *, size_t, int, const double *, size_t, double *, cudaStream_t);
+DOCI_VEC_INST(double)
+DOCI_VEC_INST(float)
+template int vec_convert<double, float>(const double *, float *, size_t, cudaStream_t);
+template int vec_convert<float, double>(const float *, double *, size_t, cudaStream_t);
+
+}  // namespace doci

@@ -1,0 +1,47 @@
+// vec.h -- launchers of the device vector layer (vec.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace doci {
+
+// partial-sum buffer size (doubles) the reductions below need
+int vec_partials_capacity();
+// out[k] = sum over blocks of partials[b][k], k < nk (device, fixed order)
+int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st);
+
+template <typename S>
+int vec_multidot(const S *V, size_t ld, int m, const S *w, size_t n, double *partials, cudaStream_t st);
+template <typename S>
+int vec_residual(const S *V, const S *VA, size_t ld, int m, const double *y, double theta, const double *diag,
+                 size_t n, S *t, double *x, double *partials, cudaStream_t st);
+template <typename S>
+int vec_gs_update(const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *partials, cudaStream_t st);
+template <typename S>
+int vec_gs_finish(const S *V, size_t ld, int m, const double *c, double scale, size_t n, const S *t, S *out,
+                  double *partials, cudaStream_t st);
+template <typename S>
+int vec_deflate(S *V, size_t ld, int mv, int keep, const double *Y, int ldy, size_t n, cudaStream_t st);
+template <typename S>
+int vec_combine(const S *V, size_t ld, int m, const double *y, size_t n, double *x, cudaStream_t st);
+template <typename A, typename B>
+int vec_convert(const A *a, B *b, size_t n, cudaStream_t st);
+
+int cg_gram(const double *x, const double *p, const double *Ax, const double *Ap, size_t n, double *partials,
+            cudaStream_t st);
+int cg_update(double a, double b, int first, double rho, double *x, const double *p, double *Ax, const double *Ap,
+              double *g, const double *pinv, size_t n, double *partials, cudaStream_t st);
+int cg_direction(double beta, int first, double *p, const double *g, size_t n, cudaStream_t st);
+int precond_inverse(const double *diag, double *pinv, size_t n, cudaStream_t st);
+
+// host-side dense symmetric eigensolver (cyclic Jacobi), ascending order;
+// A column-major n x n (leading dimension lda, upper triangle read),
+// eigenvectors to V (same leading dimension)
+void jacobi_eig(int n, const double *A, int lda, double *w, double *V);
+// lowest eigenpair of A v = lambda B v for 2x2 symmetric A, B (upper
+// triangles, column-major), B-normalised as LAPACK's dsygv returns it
+int gen_eig_2x2(const double *A, const double *B, double *lambda, double *v);
+
+}  // namespace doci

@@ -1,0 +1,196 @@
+/*
+ * doci_gb300.h -- C ABI of libdoci_gb300.so, the GB300 (sm_103a) DOCI engine.
+ *
+ * Part 1 exports the reference's own entry points (klgunst/doci) with the same
+ * names, signatures and semantics, so that its C host code (executable.c,
+ * davidson.c, CG.c) links against this library unchanged:
+ *   - the Hamiltonian / matvec plug-in of include/doci.h,
+ *   - the solver dispatch of include/wrapper_solvers.h,
+ *   - the solvers of include/davidson.h and include/CG.h,
+ *   - the FCIDUMP reader of include/read_fcidump.h.
+ * Like the reference they print the reference's messages and exit on fatal
+ * input errors.
+ *
+ * Part 2 is the status-returning API: device Hamiltonian handles, sigma on
+ * device or host buffers, the device-resident solvers (FP64 and mixed
+ * FP32/FP64), batched solves and the request server.  Every call returns a
+ * doci_status; none exits.  Streams are passed as void* (a cudaStream_t, or
+ * NULL for the handle's own stream).  No CUDA or torch types appear here.
+ */
+#ifndef DOCI_GB300_H
+#define DOCI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ======================================================================== */
+/* Part 1: reference-compatible drop-in                                      */
+/* ======================================================================== */
+
+/* include/doci.h:14, src/doci.c:69-134.  Reads the FCIDUMP, checks
+ * N_alpha == N_beta and L <= 32, builds the device Hamiltonian (addressing
+ * tables, K_ia, diagonal) and returns it through *dat.  Prints the
+ * reference's banner (doci.c:122-131). */
+void fill_doci_data(char *dumpfil, void **dat);
+
+/* include/doci.h:12, src/doci.c:136-140.  Borrowed host pointer to the D
+ * diagonal elements (owned by dat). */
+double *doci_get_diagonal(void *dat);
+
+/* include/doci.h:16, src/doci.c:142-146 */
+int doci_get_basis_size(void *dat);
+
+/* include/doci.h:18, src/doci.c:148-159.  Frees everything, sets *dat = NULL. */
+void doci_cleanup_data(void **dat);
+
+/* include/doci.h:31, src/doci.c:164-238.  result = H vec for host arrays of D
+ * doubles (they must not alias); result is overwritten.  FP64 on the GPU,
+ * host<->device copies inside the call. */
+void doci_matvec(double *vec, double *result, void *dat);
+
+/* include/wrapper_solvers.h:36-38, src/wrapper_solvers.c:10-24.
+ * solver "D" (Davidson), "CG", "CGP" (CG, diagonal preconditioner); M must be
+ * NULL.  When matvec == doci_matvec and dat came from fill_doci_data the whole
+ * solve stays on the device; any other matvec is called on host buffers once
+ * per iteration while the vector layer runs on the device.  Returns -1 for an
+ * unknown solver, else the solver's return value. */
+int sparse_eigensolve(double *vec, int dims, double *energy,
+                      void (*matvec)(double *, double *, void *), double *diagonal,
+                      double *M, double tol, int max_its, char solver[],
+                      int davidson_keep, int davidson_max_vec, void *dat);
+
+/* include/davidson.h:25-27, src/davidson.c:33-128.  Returns its >= max_its. */
+int davidson(double *result, double *energy, int max_vectors, int keep_deflate,
+             double davidson_tol, void (*matvec)(double *, double *, void *),
+             double *diagonal, int basis_size, int max_its, void *vdat);
+
+/* include/CG.h:4-5, src/CG.c:13-164.  Returns its <= max_its (as the
+ * reference, this is 1 even when MAX_ITS was reached). */
+int ray_q(void (*matvec)(double *, double *, void *), double *M, double *vec, int size,
+          double *energy, double cg_tol, int max_its, double *precond, void *vdat);
+
+/* include/read_fcidump.h:4, src/read_fcidump.c:18-82.  Allocates one_p_int
+ * (L*L) and two_p_int (L^4) with malloc; the caller frees them. */
+void read_fcidump(char *filename, unsigned int *NORB, unsigned int *NALPHA,
+                  unsigned int *NBETA, double *core_energy, double **one_p_int,
+                  double **two_p_int);
+
+/* ======================================================================== */
+/* Part 2: status-returning GB300 API                                        */
+/* ======================================================================== */
+
+typedef enum doci_status {
+  DOCI_OK = 0,
+  DOCI_ERR_OPEN = 1,              /* FCIDUMP cannot be opened (read_fcidump.c:27-30) */
+  DOCI_ERR_FORMAT = 2,            /* malformed header or integral line (:33-42, :63-67) */
+  DOCI_ERR_NALPHA_NBETA = 3,      /* N_alpha != N_beta (doci.c:76-82) */
+  DOCI_ERR_TOO_MANY_ORBITALS = 4, /* L > 32 (doci.c:84-89) */
+  DOCI_ERR_INVALID = 5,           /* bad argument */
+  DOCI_ERR_CUDA = 6,              /* a CUDA call failed */
+  DOCI_ERR_OUT_OF_MEMORY = 7,     /* device or host allocation failed */
+  DOCI_ERR_NO_DEVICE = 8,         /* no CUDA device */
+  DOCI_ERR_ADMISSION = 9,         /* request larger than the server's HBM budget */
+  DOCI_ERR_NOT_FOUND = 10,        /* unknown ticket */
+  DOCI_ERR_PENDING = 11,          /* ticket not finished yet */
+  DOCI_ERR_DEVICE_TIMEOUT = 12,   /* a bounded device wait ran out */
+  DOCI_ERR_UNKNOWN_SOLVER = 13
+} doci_status;
+
+typedef enum doci_precision {
+  DOCI_FP64 = 0, /* FP64 storage and arithmetic */
+  DOCI_FP32 = 1  /* FP32 storage, FP32 sigma with FP32 accumulation */
+} doci_precision;
+
+/* Opaque device Hamiltonian: integrals, addressing tables and diagonal,
+ * resident on one GPU. */
+typedef struct doci_ham doci_ham;
+
+const char *doci_status_string(int status);
+
+/* Build from an FCIDUMP file (same parser and integral transform as the
+ * reference: read_fcidump.c:18-82, doci.c:630-665). */
+int doci_ham_from_fcidump(const char *path, doci_ham **out);
+
+/* Build from integrals laid out as read_fcidump returns them (before the
+ * transform): one[L*L], two[L^4] with two[i + j L + k L^2 + l L^3] = (ij|kl),
+ * 0-based, canonical entries at least (the transform mirrors them). */
+int doci_ham_from_integrals(int L, int n_pairs, double core, const double *one,
+                            const double *two, doci_ham **out);
+
+void doci_ham_destroy(doci_ham *ham);
+
+/* L, N (pairs), D = C(L, N) */
+int doci_ham_dims(const doci_ham *ham, int *L, int *n_pairs, int64_t *dim);
+
+/* Copy the FP64 diagonal (doci.c:550-628, bit-identical summation order) to
+ * host memory out[D]. */
+int doci_ham_diagonal(const doci_ham *ham, double *out);
+
+/* Device pointer to the FP64 diagonal (borrowed). */
+const double *doci_ham_diagonal_device(const doci_ham *ham);
+
+/* sigma = H x on device buffers of D elements (double for DOCI_FP64, float
+ * for DOCI_FP32).  y is overwritten; x and y must not alias.  Asynchronous on
+ * stream (NULL = the handle's stream). */
+int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *stream);
+
+/* Same on host buffers; copies in and out inside the call, synchronous. */
+int doci_sigma_host(doci_ham *ham, const void *x, void *y, int precision);
+
+/* Lexical addressing on the device: bitstrings of determinants
+ * [first, first+count) (bit o = orbital o, order of doci.c:472-548), and the
+ * inverse map from bitstrings to ranks. */
+int doci_bitstrings(doci_ham *ham, int64_t first, int64_t count, uint32_t *d_bits, void *stream);
+int doci_ranks(doci_ham *ham, const uint32_t *d_bits, int64_t count, int64_t *d_ranks, void *stream);
+
+typedef enum doci_solver_kind { DOCI_SOLVER_D = 0, DOCI_SOLVER_CG = 1, DOCI_SOLVER_CGP = 2 } doci_solver_kind;
+
+typedef enum doci_solve_mode {
+  DOCI_MODE_FP64 = 0,  /* FP64 sigma and FP64 basis throughout */
+  DOCI_MODE_MIXED = 1  /* FP32 sigma and FP32 basis (FP64 reductions, GS, residual,
+                          subspace), then FP64 Davidson steps from that vector */
+} doci_solve_mode;
+
+typedef struct doci_solve_opts {
+  int solver;            /* doci_solver_kind (input key SOLVER) */
+  int max_its;           /* MAX_ITS, default 200 (options.h:7) */
+  double tol;            /* TOL, default 1e-8 (options.h:6) */
+  int davidson_keep;     /* DAVIDSON_KEEP, default 2 (options.h:5) */
+  int davidson_max_vec;  /* DAVIDSON_MAX_VEC, default 30 (options.h:4) */
+  int hf_init;           /* HF_INIT, default 1; 0 = seeded random start */
+  int mode;              /* doci_solve_mode (Davidson only) */
+  double mixed_tol;      /* residual at which the FP32 phase hands over (mixed) */
+  int print_level;       /* 0 silent, 1 reference summary lines, 2 per-iteration table */
+  uint64_t seed;         /* random start seed (hf_init == 0) */
+} doci_solve_opts;
+
+typedef struct doci_solve_result {
+  double energy;         /* lowest eigenvalue */
+  double residual;       /* final ||H x - E x||_2 (Davidson) or ||g||^2 (CG) */
+  int iterations;        /* total solver iterations (one sigma each) */
+  int iterations_fp32;   /* of which in the FP32 phase (mixed mode) */
+  int converged;         /* residual criterion met within max_its */
+  int status_code;       /* reference-style return code of the solver */
+  double energy_fp32;    /* energy at the end of the FP32 phase (mixed) */
+  double seconds;        /* wall time of the solve */
+  double sigma_seconds;  /* device time spent in sigma */
+} doci_solve_result;
+
+void doci_solve_opts_default(doci_solve_opts *opts);
+
+/* Device-resident solve.  vec (host, D doubles) may be NULL; when given it is
+ * the start vector if opts->hf_init < 0, and receives the eigenvector. */
+int doci_solve(doci_ham *ham, const doci_solve_opts *opts, double *vec,
+               doci_solve_result *result);
+
+/* Bytes of device memory a solve of ham with opts needs (admission). */
+int64_t doci_solve_footprint(int L, int n_pairs, const doci_solve_opts *opts, int nroots);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,33 @@
+"""CPU check of the sigma kernels' neighbour-rank arithmetic: the device
+enumeration code (addressing.cuh) compiled for the host and run over whole
+small spaces and sampled large ones (every index in range and equal to the
+direct lexical rank; every hop visited once)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "host_checks", "neighbours_check.cu")
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    out = str(tmp_path_factory.mktemp("nb") / "neighbours_check")
+    subprocess.run([nvcc, "-O2", "-std=c++17", SRC, "-o", out], check=True)
+    return out
+
+
+@pytest.mark.parametrize("L,N,stride", [
+    (1, 0, 1), (1, 1, 1), (4, 2, 1), (7, 3, 1), (10, 5, 1), (12, 1, 1), (12, 11, 1), (14, 7, 1),
+    (16, 8, 1), (18, 5, 1), (20, 10, 7), (24, 12, 4099), (28, 14, 100003), (28, 7, 997), (32, 16, 1000003),
+    (32, 1, 1), (32, 31, 1), (32, 2, 3), (32, 30, 3), (31, 15, 700001), (32, 0, 1), (32, 32, 1),
+])
+def test_neighbour_ranks(exe, L, N, stride):
+    r = subprocess.run([exe, str(L), str(N), str(stride)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad=0" in r.stdout
