@@ -203,8 +203,11 @@ def main():
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
     x = torch.randn(D, dtype=tdt, device="cuda", generator=g)
     y = torch.empty_like(x)
-    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    # a dedicated stream: the sigma launches and the CUDA events share it
+    stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
+    assert sptr != 0
     for _ in range(a.warmup):
         h.sigma_device(x.data_ptr(), y.data_ptr(), prec, sptr)
     torch.cuda.synchronize()

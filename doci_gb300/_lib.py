@@ -84,6 +84,7 @@ def lib() -> C.CDLL:
         "doci_sigma_host": (i, [vp, vp, vp, i]),
         "doci_bitstrings": (i, [vp, i64, i64, vp, vp]),
         "doci_ranks": (i, [vp, vp, i64, vp, vp]),
+        "doci_multidot": (i, [vp, i64, i, vp, i64, i, vp, vp]),
         "doci_solve_opts_default": (None, [C.POINTER(SolveOpts)]),
         "doci_solve": (i, [vp, C.POINTER(SolveOpts), pd, C.POINTER(SolveResult)]),
         "doci_solve_footprint": (i64, [i, i, C.POINTER(SolveOpts), i]),

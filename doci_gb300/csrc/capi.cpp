@@ -191,6 +191,25 @@ int doci_ranks(doci_ham *h, const uint32_t *d_bits, int64_t count, int64_t *d_ra
   return launch_ranks(h, d_bits, count, d_ranks, pick(h, stream));
 }
 
+int doci_multidot(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n, int precision, double *d_out,
+                  void *stream) {
+  if (!d_V || !d_w || !d_out || m < 1 || m > 32 || n < 0 || ld < n) return DOCI_ERR_INVALID;
+  if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double *partials = nullptr;
+  DOCI_CUDA(cudaMallocAsync(&partials, sizeof(double) * vec_partials_capacity(), st));
+  int s = precision == DOCI_FP64
+              ? vec_multidot<double>(static_cast<const double *>(d_V), static_cast<size_t>(ld), m,
+                                     static_cast<const double *>(d_w), static_cast<size_t>(n), partials, st)
+              : vec_multidot<float>(static_cast<const float *>(d_V), static_cast<size_t>(ld), m,
+                                    static_cast<const float *>(d_w), static_cast<size_t>(n), partials, st);
+  if (s == DOCI_OK) s = vec_reduce(partials, m, d_out, st);
+  const cudaError_t e = cudaFreeAsync(partials, st);
+  if (s != DOCI_OK) return s;
+  DOCI_CUDA(e);
+  return DOCI_OK;
+}
+
 void doci_solve_opts_default(doci_solve_opts *o) {
   if (!o) return;
   std::memset(o, 0, sizeof *o);
@@ -387,6 +406,7 @@ void fill_doci_data(char *dumpfil, void **dat) {
       "\t** basis size : %u\n"
       "----------\n",
       dev, prop.name, sms, h->N, h->N, h->L, h->D);
+  std::fflush(stdout);
   *dat = h;
 }
 

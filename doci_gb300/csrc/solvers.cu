@@ -200,6 +200,7 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
   } else if (a.print_summary) {
     std::printf("\t\t ** DAVIDSON ITERATIONS : %d\n", its);
   }
+  std::fflush(stdout);
   // the eigenvector x = V y of the last Ritz pair
   if (d_x_out) {
     DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
@@ -288,6 +289,7 @@ int ray_q_run(MatvecOp &op, size_t D, const double *d_diag_or_null, double *d_x,
       std::printf("CG didn't converge within %d iterations! d_energy is %e.\n", a.max_its, d_energy);
     std::printf("elapsed time : %lf sec\n", t1 - t0);
     std::printf("average time per matvec : %lf sec\n", (t1 - t0) / (its + 1));
+    std::fflush(stdout);
   }
   out->energy = rho;
   out->normq = normq;

@@ -147,6 +147,18 @@ int doci_sigma_host(doci_ham *ham, const void *x, void *y, int precision);
 int doci_bitstrings(doci_ham *ham, int64_t first, int64_t count, uint32_t *d_bits, void *stream);
 int doci_ranks(doci_ham *ham, const uint32_t *d_bits, int64_t count, int64_t *d_ranks, void *stream);
 
+/* Projections out[i] = V_i . w for i < m (m <= 32) on device buffers: V is
+ * column-major with leading dimension ld >= n (element type double for
+ * DOCI_FP64, float for DOCI_FP32), w has n elements, out is m doubles on the
+ * device.  Products are accumulated in FP64 in a fixed order (per-block
+ * partial sums, then one block adding them), so repeated calls give identical
+ * results.  This is the subspace-column / Gram-Schmidt reduction of the
+ * Davidson vector layer (davidson.c:139-143, :178-193: m ddot_ calls in the
+ * reference), for callers that run their own solver around doci_sigma.
+ * Allocates its partial-sum scratch on `stream` (stream-ordered). */
+int doci_multidot(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n, int precision, double *d_out,
+                  void *stream);
+
 typedef enum doci_solver_kind { DOCI_SOLVER_D = 0, DOCI_SOLVER_CG = 1, DOCI_SOLVER_CGP = 2 } doci_solver_kind;
 
 typedef enum doci_solve_mode {
