@@ -81,6 +81,25 @@ def workload_path(L: int, N: int, seed: int, rank: int, ws: int) -> str:
     return p
 
 
+def max_over_ranks(x: float, ws: int) -> float:
+    """The slowest rank's time (replicas: no collective in the data path;
+    this is the only cross-rank operation)."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_gdets(dets_per_rank: int, steps: int, ws: int, seconds: float) -> float:
+    """Whole-job determinants per second: every rank processed its own
+    replica's dets_per_rank x steps in at most `seconds`."""
+    return dets_per_rank * steps * ws / seconds / 1e9
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -231,12 +250,8 @@ def main():
         dist.barrier()
     clk = clocks.stop()
     per_launch = [ev[k].elapsed_time(ev[k + 1]) * 1e-3 for k in range(a.steps)]
-    total = ev[0].elapsed_time(ev[a.steps]) * 1e-3
-    if ws > 1:
-        t = torch.tensor([total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
-    value = D * a.steps * ws / total / 1e9
+    total = max_over_ranks(ev[0].elapsed_time(ev[a.steps]) * 1e-3, ws)
+    value = replica_gdets(D, a.steps, ws, total)
     mean_launch = statistics.mean(per_launch)
     bytes_alg = D * (esize + esize + esize)  # x, diagonal, sigma
     peaks, peak_kind = measured_peaks()
@@ -264,12 +279,8 @@ def main():
         for _ in range(a.e2e_steps):
             st = lib.doci_sigma_host(h.handle, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()), prec)
             assert st == 0, st
-        te = time.perf_counter() - t0
-        if ws > 1:
-            t = torch.tensor([te], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
-        e2e = {"value": round(D * a.e2e_steps * ws / te / 1e9, 4), "unit": UNIT,
+        te = max_over_ranks(time.perf_counter() - t0, ws)
+        e2e = {"value": round(replica_gdets(D, a.e2e_steps, ws, te), 4), "unit": UNIT,
                "h2d_bytes_per_step": D * esize, "d2h_bytes_per_step": D * esize,
                "call": "doci_sigma_host (C ABI, pinned host buffers)", "steps": a.e2e_steps}
     cpu = None
