@@ -109,6 +109,7 @@ const char *doci_status_string(int s) {
     case DOCI_ERR_PENDING: return "not finished";
     case DOCI_ERR_DEVICE_TIMEOUT: return "device wait timed out";
     case DOCI_ERR_UNKNOWN_SOLVER: return "unknown solver";
+    case DOCI_ERR_SCRATCH_LIMIT: return "request exceeds the fixed scratch of the allocation-free entry point";
     default: return "unknown status";
   }
 }

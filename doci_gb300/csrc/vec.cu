@@ -406,6 +406,8 @@ struct CombineL {
 
 int vec_partials_capacity() { return grid_blocks() * kMaxK; }
 
+int vec_reduction_blocks() { return grid_blocks(); }
+
 int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st) {
   reduce_partials_kernel<<<1, kT, 0, st>>>(partials, grid_blocks(), nk, out);
   DOCI_CUDA(cudaGetLastError());

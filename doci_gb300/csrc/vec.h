@@ -9,6 +9,8 @@ namespace doci {
 
 // partial-sum buffer size (doubles) the reductions below need
 int vec_partials_capacity();
+// number of blocks (rows of partial sums) every reduction kernel launches
+int vec_reduction_blocks();
 // out[k] = sum over blocks of partials[b][k], k < nk (device, fixed order)
 int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st);
 

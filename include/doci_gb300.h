@@ -97,7 +97,8 @@ typedef enum doci_status {
   DOCI_ERR_NOT_FOUND = 10,        /* unknown ticket */
   DOCI_ERR_PENDING = 11,          /* ticket not finished yet */
   DOCI_ERR_DEVICE_TIMEOUT = 12,   /* a bounded device wait ran out */
-  DOCI_ERR_UNKNOWN_SOLVER = 13
+  DOCI_ERR_UNKNOWN_SOLVER = 13,
+  DOCI_ERR_SCRATCH_LIMIT = 14     /* request exceeds the fixed scratch of doci_multidot_noalloc */
 } doci_status;
 
 typedef enum doci_precision {
@@ -158,6 +159,24 @@ int doci_ranks(doci_ham *ham, const uint32_t *d_bits, int64_t count, int64_t *d_
  * Allocates its partial-sum scratch on `stream` (stream-ordered). */
 int doci_multidot(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n, int precision, double *d_out,
                   void *stream);
+
+/* doci_multidot without any device allocation.  No counterpart in the
+ * reference: it serves callers that cannot let a library allocate GPU
+ * memory -- processes that keep the device's memory in their own
+ * pre-reserved pool (a serving loop holding many resident Davidson states,
+ * a framework's caching allocator), where an extra cudaMalloc can fail or
+ * fragment the pool, and latency-critical loops that cannot afford the
+ * synchronisation an allocation or free may cause.  Same arguments and
+ * results as doci_multidot; the per-block partial sums live in a fixed
+ * 256 KiB array in the library's device image, held on every GPU that loads
+ * the library until the process exits.  Limit: m <= 32 (larger m returns
+ * DOCI_ERR_SCRATCH_LIMIT).  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress), so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller.  Allocates nothing, frees nothing. */
+int doci_multidot_noalloc(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n, int precision,
+                          double *d_out, void *stream);
 
 typedef enum doci_solver_kind { DOCI_SOLVER_D = 0, DOCI_SOLVER_CG = 1, DOCI_SOLVER_CGP = 2 } doci_solver_kind;
 
