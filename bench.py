@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--N", type=int, default=16)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--kernel", choices=["auto", "gather", "row"], default="auto")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -218,6 +219,7 @@ def main():
     tdt = torch.float32 if prec == dg.FP32 else torch.float64
     esize = 4 if prec == dg.FP32 else 8
     h = dg.Hamiltonian.from_fcidump(path)
+    h.set_sigma_kernel(a.kernel)
     D = h.D
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
     x = torch.randn(D, dtype=tdt, device="cuda", generator=g)

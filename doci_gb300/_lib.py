@@ -82,6 +82,7 @@ def lib() -> C.CDLL:
         "doci_ham_diagonal_device": (vp, [vp]),
         "doci_sigma": (i, [vp, vp, vp, i, vp]),
         "doci_sigma_host": (i, [vp, vp, vp, i]),
+        "doci_ham_set_sigma_kernel": (i, [vp, i]),
         "doci_bitstrings": (i, [vp, i64, i64, vp, vp]),
         "doci_ranks": (i, [vp, vp, i64, vp, vp]),
         "doci_multidot": (i, [vp, i64, i, vp, i64, i, vp, vp]),
@@ -173,6 +174,11 @@ class Hamiltonian:
 
     def __exit__(self, *a):
         self.close()
+
+    def set_sigma_kernel(self, kind) -> None:
+        """0/'auto', 1/'gather', 2/'row'."""
+        kind = {"auto": 0, "gather": 1, "row": 2}.get(kind, kind)
+        _check(lib().doci_ham_set_sigma_kernel(self._h, int(kind)), "doci_ham_set_sigma_kernel")
 
     def diagonal(self) -> np.ndarray:
         out = np.empty(self.D, dtype=np.float64)

@@ -135,5 +135,67 @@ struct Neighbours {
   }
 };
 
+// One column of a row in the row-tiled sigma (mirrored orbitals [0, sp) =
+// column part, [sp, L) = row part).  The row has row-part occupation R with
+// j = N - |R| elements left for the column part, n = C(sp, j) columns;
+// column c holds the column-part set of colex n-1-c.  Calls
+//   f.inrow(m, q, c')      hop m -> q inside the column part: column c' of this row
+//   f.up(t, m, q, c')      hop of row-part element ab_m[t] = m to column-part hole q:
+//                          column c' of row R \ m (start ab_rs[t])
+//   f.down(t, m, q, c')    hop of column-part element m to row-part hole ba_q[t] = q:
+//                          column c' of row R u q
+//   f.across(t, c)         row-part hop t (table entry): same column c of another row
+template <int NHB, int BC, typename F>
+DOCI_HD void row_column_hops(uint32_t c, uint32_t n, int sp, int j, const uint32_t *B, int n_ab, const int *ab_m,
+                             int n_ba, const int *ba_q, int n_aa, F &f) {
+  const uint32_t p = n - 1 - c;
+  const uint32_t Mb = colex_unrank<BC>(p, sp, j, B);
+  Neighbours<NHB, BC> nb;
+  nb.precompute(Mb, p, sp, sp - j, B);
+  const int nhB = sp - j;
+  const uint32_t n_up_m1 = (j < sp ? B[sp * BC + j + 1] : 1u) - 1u;
+  const uint32_t n_dn_m1 = (j > 0 ? B[sp * BC + j - 1] : 1u) - 1u;
+  uint32_t PVtot = 0, PUtot = 0;
+  {
+    uint32_t mr = Mb;
+    for (int i = 0; i < j; ++i) {
+      const int m = ffs32(mr) - 1;
+      mr &= mr - 1;
+      PVtot += B[m * BC + i + 2];
+      PUtot += B[m * BC + i];
+    }
+  }
+  uint32_t mrem = Mb, PW = 0, PU = 0, PV = 0;
+  for (int kk = 0; kk < j; ++kk) {
+    const int m = ffs32(mrem) - 1;
+    mrem &= mrem - 1;
+    const uint32_t W = B[m * BC + kk + 1], U = B[m * BC + kk], V = B[m * BC + kk + 2];
+    const uint32_t base1 = n - 1 - (PV + p - (PW + W));
+    const uint32_t base2 = n - 1 - (PW - (PU + U));
+    f.begin(m);
+#pragma unroll
+    for (int h = 0; h < NHB; ++h) {
+      if (h < nhB) f.inrow(m, nb.Q[h], nb.Q[h] < m ? base1 - nb.E1[h] : base2 - nb.E2[h]);
+    }
+    // colex(M_B \ m) = PW(kk) + PUtot - PU(kk+1)
+    const uint32_t cdn = n_dn_m1 - (PW + PUtot - (PU + U));
+    for (int t = 0; t < n_ba; ++t) f.down(t, m, ba_q[t], cdn);
+    PW += W;
+    PU += U;
+    PV += V;
+  }
+  if (n_ab > 0) {
+#pragma unroll
+    for (int h = 0; h < NHB; ++h) {
+      if (h < nhB) {
+        // colex(M_B u q) = E1[h] + PVtot
+        const uint32_t cup = n_up_m1 - (nb.E1[h] + PVtot);
+        for (int t = 0; t < n_ab; ++t) f.up(t, ab_m[t], nb.Q[h], cup);
+      }
+    }
+  }
+  for (int t = 0; t < n_aa; ++t) f.across(t, c);
+}
+
 }  // namespace dev
 }  // namespace doci

@@ -168,6 +168,12 @@ int doci_sigma(doci_ham *h, const void *d_x, void *d_y, int precision, void *str
   return launch_sigma(h, d_x, d_y, precision, pick(h, stream));
 }
 
+int doci_ham_set_sigma_kernel(doci_ham *h, int kind) {
+  if (!h || kind < 0 || kind > 2) return DOCI_ERR_INVALID;
+  h->sigma_kernel = kind;
+  return DOCI_OK;
+}
+
 int doci_sigma_host(doci_ham *h, const void *x, void *y, int precision) {
   if (!h || !x || !y || x == y) return DOCI_ERR_INVALID;
   if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;

@@ -8,7 +8,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
+#include <utility>
 
 #include "internal.h"
 
@@ -48,6 +50,9 @@ void ham_release(doci_ham *h) {
   cudaFree(h->d_diag32);
   cudaFree(h->d_stage_x);
   cudaFree(h->d_stage_y);
+  cudaFree(h->d_rows);
+  cudaFree(h->d_rowstart);
+  h->d_rows = h->d_rowstart = nullptr;
   if (h->h_diag) cudaFreeHost(h->h_diag);
   if (h->stream) cudaStreamDestroy(h->stream);
   h->d_binom = nullptr;
@@ -132,6 +137,72 @@ int ham_build(doci_ham *h, const Integrals &in) {
   DOCI_CUDA(cudaMemcpyAsync(h->d_tab64, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   int st = launch_diagonal(h, h->stream);
   if (st) return st;
+  st = ham_build_rows(h);
+  if (st) return st;
+  DOCI_CUDA(cudaStreamSynchronize(h->stream));
+  return DOCI_OK;
+}
+
+// Row table for the row sigma kernel.  The column part takes the lowest
+// `split` mirrored orbitals (split <= 16, so a row of C(split, j) elements
+// fits in shared memory); the split shrinks until there are enough rows to
+// spread over the SMs.  For a row-part occupation R (bit a = mirrored
+// orbital split + a) with k elements and j = N - k in the column part, the
+// colex ranks of the row are [base, base + C(split, j)) with
+// base = sum_t C(split + a_t, j + t + 1) over R's elements a_0 < a_1 < ...,
+// i.e. ranks [D - base - C(split, j), D - 1 - base].
+int ham_build_rows(doci_ham *h) {
+  const int L = h->L, N = h->N;
+  int split = L < 16 ? L : 16;
+  auto count_rows = [&](int sp) {
+    const int na = L - sp;
+    long n = 0;
+    for (int k = 0; k <= na; ++k) {
+      const int j = N - k;
+      if (j >= 0 && j <= sp) n += static_cast<long>(binom64(na, k));
+    }
+    return n;
+  };
+  while (split > 8 && count_rows(split) < 8L * device_sm_count()) --split;
+  const int na = L - split;
+  if (na > 24) return DOCI_ERR_INVALID;
+  h->split = split;
+  std::vector<uint32_t> rows, start(size_t(1) << na, 0xffffffffu);
+  int max_row = 0;
+  for (uint32_t mask = 0; mask < (1u << na); ++mask) {
+    const int k = __builtin_popcount(mask);
+    const int j = N - k;
+    if (j < 0 || j > split) continue;
+    uint64_t base = 0;
+    int t = 0;
+    for (int a = 0; a < na; ++a)
+      if (mask >> a & 1u) {
+        base += binom64(split + a, j + t + 1);
+        ++t;
+      }
+    const uint64_t len = binom64(split, j);
+    const uint64_t rs = static_cast<uint64_t>(h->D) - base - len;
+    start[mask] = static_cast<uint32_t>(rs);
+    rows.push_back(static_cast<uint32_t>(rs));
+    rows.push_back(mask | (static_cast<uint32_t>(k) << 24));
+    if (static_cast<int>(len) > max_row) max_row = static_cast<int>(len);
+  }
+  // process rows in rank order
+  std::vector<std::pair<uint32_t, uint32_t>> order;
+  for (size_t i = 0; i < rows.size(); i += 2) order.emplace_back(rows[i], rows[i + 1]);
+  std::sort(order.begin(), order.end());
+  rows.clear();
+  for (auto &p : order) {
+    rows.push_back(p.first);
+    rows.push_back(p.second);
+  }
+  h->nrows = static_cast<int>(order.size());
+  h->max_row = max_row;
+  DOCI_CUDA(cudaMalloc(&h->d_rows, rows.size() * sizeof(uint32_t)));
+  DOCI_CUDA(cudaMalloc(&h->d_rowstart, start.size() * sizeof(uint32_t)));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_rows, rows.data(), rows.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_rowstart, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                            h->stream));
   DOCI_CUDA(cudaStreamSynchronize(h->stream));
   return DOCI_OK;
 }

@@ -74,6 +74,17 @@ struct doci_ham {
   double *d_diag = nullptr;      // D, FP64 diagonal
   float *d_diag32 = nullptr;     // D, FP32 copy
 
+  // Row tiling of the rank space used by the row sigma kernel: mirrored
+  // orbitals [0, split) are the "column" part, [split, L) the "row" part.
+  // All determinants with the same row-part occupation form one contiguous
+  // rank range (a row) of C(split, j) columns, j = N - |row part|.
+  int split = 0;                  // columns' orbitals; 0 = row kernel unused
+  int nrows = 0;
+  int max_row = 0;                // largest row length
+  uint32_t *d_rows = nullptr;     // nrows x {rowstart, mask | k << 24}
+  int sigma_kernel = 0;           // 0 automatic, 1 per-determinant gather, 2 row kernel
+  uint32_t *d_rowstart = nullptr; // 2^(L - split) entries: row start by row-part mask
+
   // host diagonal for doci_get_diagonal (lazy)
   double *h_diag = nullptr;
   // device staging for the host-buffer entry points (lazy)
@@ -93,4 +104,5 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
 int launch_bitstrings(const doci_ham *h, int64_t first, int64_t count, uint32_t *out, cudaStream_t s);
 int launch_ranks(const doci_ham *h, const uint32_t *bits, int64_t count, int64_t *out, cudaStream_t s);
 int launch_diagonal(doci_ham *h, cudaStream_t s);
+int ham_build_rows(doci_ham *h);
 }  // namespace doci

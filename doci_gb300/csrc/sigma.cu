@@ -10,6 +10,8 @@
 // no partial vectors, sigma written once with coalesced stores.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "addressing.cuh"
 #include "internal.h"
 
@@ -163,6 +165,159 @@ __global__ void ranks_kernel(SigmaShape s, const uint32_t *__restrict__ g_binom,
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Row kernel.  Mirrored orbitals [0, split) form the column part, [split, L)
+// the row part.  A row (fixed row-part occupation R, k elements; j = N - k in
+// the column part) is a contiguous rank range of n = C(split, j) determinants;
+// column c of the row holds colex_B = n - 1 - c of its column-part set.  One
+// block handles one row at a time: it stages x[row] in shared memory and every
+// thread computes whole columns, split into the four hop classes:
+//   column part -> column part : gathers from the staged row (shared memory);
+//   row part    -> row part    : the same column of another row of the same
+//                                length (one coalesced load per hop);
+//   row part    -> column part : column c' of row R\m (one more column element,
+//                                colex of M_B u q = E1[h] + PVtot);
+//   column part -> row part    : column c' of row R u q (colex of
+//                                M_B \ m_k = PW(k) + PUtot - PU(k+1)).
+// The rows' starts come from a table indexed by the row-part mask.
+// ---------------------------------------------------------------------------
+constexpr int kRowThreads = 256;
+constexpr int kMaxRowPart = 24;                  // L - split
+constexpr int kMaxIntraRow = 12 * 12;            // k (na - k) <= (na / 2)^2
+
+struct RowShape {
+  uint32_t D;
+  int L, N, split, na, nrows;
+};
+
+template <typename Real>
+struct RowTables {
+  uint32_t binom[kBinomRows * kBinomCols];
+  Real K[32 * 32];
+  uint32_t aa_rs[kMaxIntraRow];  // row part -> row part: start of R \ m u q
+  Real aa_K[kMaxIntraRow];
+  uint32_t ab_rs[kMaxRowPart];   // row part -> column part: start of R \ m
+  int ab_m[kMaxRowPart];
+  uint32_t ba_rs[kMaxRowPart];   // column part -> row part: start of R u q
+  int ba_q[kMaxRowPart];
+  int n_aa, n_ab, n_ba;
+};
+
+template <typename Real, int NHB>
+__global__ void __launch_bounds__(kRowThreads)
+sigma_row_kernel(RowShape s, const uint2 *__restrict__ rows, const uint32_t *__restrict__ rowstart_of,
+                 const uint32_t *__restrict__ g_binom, const Real *__restrict__ g_K, const Real *__restrict__ diag,
+                 const Real *__restrict__ x, Real *__restrict__ y) {
+  __shared__ RowTables<Real> tb;
+  extern __shared__ __align__(16) unsigned char row_smem[];
+  Real *xs = reinterpret_cast<Real *>(row_smem);
+  for (int t = threadIdx.x; t < kBinomRows * kBinomCols; t += blockDim.x) tb.binom[t] = g_binom[t];
+  for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) tb.K[t] = g_K[t];
+  const uint32_t *B = tb.binom;
+  const int sp = s.split, na = s.na;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  for (int row = blockIdx.x; row < s.nrows; row += gridDim.x) {
+    const uint2 rw = rows[row];
+    const uint32_t rstart = rw.x, mask = rw.y & 0xffffffu;
+    const int k = static_cast<int>(rw.y >> 24), j = s.N - k;
+    __syncthreads();  // previous row finished with xs and the tables
+    if (warp == 0) {
+      // row-part elements and holes, compacted with ballots
+      const bool live = lane < na;
+      const bool in_r = live && ((mask >> lane) & 1u);
+      const bool hole = live && !in_r;
+      const uint32_t eb = __ballot_sync(0xffffffffu, in_r), hb = __ballot_sync(0xffffffffu, hole);
+      const uint32_t below = (1u << lane) - 1u;
+      if (in_r) {
+        const int e = __popc(eb & below);
+        tb.ab_rs[e] = rowstart_of[mask & ~(1u << lane)];
+        tb.ab_m[e] = sp + lane;
+      }
+      if (hole) {
+        const int h = __popc(hb & below);
+        tb.ba_rs[h] = rowstart_of[mask | (1u << lane)];
+        tb.ba_q[h] = sp + lane;
+      }
+      const int ne = __popc(eb), nhl = __popc(hb);
+      if (lane == 0) {
+        tb.n_ab = j < sp ? ne : 0;   // a column-part hole must exist
+        tb.n_ba = j > 0 ? nhl : 0;   // a column-part element must exist
+        tb.n_aa = ne * nhl;
+      }
+      // row part -> row part pairs (element e, hole h)
+      for (int t = lane; t < ne * nhl; t += 32) {
+        const int e = t / nhl, h = t % nhl;
+        const int a_e = __fns(eb, 0, e + 1), a_h = __fns(hb, 0, h + 1);
+        tb.aa_rs[t] = rowstart_of[(mask & ~(1u << a_e)) | (1u << a_h)];
+        tb.aa_K[t] = g_K[(sp + a_e) * 32 + sp + a_h];
+      }
+    }
+    const uint32_t n = B[sp * kBinomCols + j];
+    for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) xs[c] = x[rstart + c];
+    __syncthreads();
+
+    const int n_aa = tb.n_aa, n_ab = tb.n_ab, n_ba = tb.n_ba;
+    struct Acc {
+      const RowTables<Real> &tb;
+      const Real *xs, *x;
+      const Real *Krow;
+      Real acc;
+      __device__ __forceinline__ void begin(int m) { Krow = tb.K + m * 32; }
+      __device__ __forceinline__ void inrow(int, int q, uint32_t cc) { acc += Krow[q] * xs[cc]; }
+      __device__ __forceinline__ void down(int t, int, int q, uint32_t cc) {
+        acc += Krow[q] * __ldg(x + tb.ba_rs[t] + cc);
+      }
+      __device__ __forceinline__ void up(int t, int m, int q, uint32_t cc) {
+        acc += tb.K[m * 32 + q] * __ldg(x + tb.ab_rs[t] + cc);
+      }
+      __device__ __forceinline__ void across(int t, uint32_t cc) { acc += tb.aa_K[t] * __ldg(x + tb.aa_rs[t] + cc); }
+    };
+    for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) {
+      Acc f{tb, xs, x, tb.K, diag[rstart + c] * xs[c]};
+      dev::row_column_hops<NHB, kBinomCols>(c, n, sp, j, B, n_ab, tb.ab_m, n_ba, tb.ba_q, n_aa, f);
+      y[rstart + c] = f.acc;
+    }
+  }
+}
+
+template <typename Real>
+int launch_row(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
+  const RowShape s{h->D, h->L, h->N, h->split, h->L - h->split, h->nrows};
+  const size_t dyn = static_cast<size_t>(h->max_row) * sizeof(Real);
+  auto kern = sigma_row_kernel<Real, 16>;
+  static int blocks_per_sm = 0;
+  static size_t configured = 0;
+  if (configured != dyn) {
+    DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    blocks_per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kRowThreads, dyn);
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    configured = dyn;
+  }
+  int grid = device_sm_count() * blocks_per_sm;
+  if (grid > h->nrows) grid = h->nrows;
+  const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
+                                                   : reinterpret_cast<const Real *>(h->d_Kmir32);
+  const Real *dg = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_diag)
+                                                    : reinterpret_cast<const Real *>(h->d_diag32);
+  kern<<<grid, kRowThreads, dyn, st>>>(s, reinterpret_cast<const uint2 *>(h->d_rows), h->d_rowstart, h->d_binom, K,
+                                       dg, static_cast<const Real *>(x), static_cast<Real *>(y));
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+bool row_kernel_fits(const doci_ham *h, size_t elem) {
+  if (h->split < 1 || h->nrows < 1) return false;
+  if (h->L - h->split > kMaxRowPart || (h->L - h->split) > 32) return false;
+  if (h->split - 0 > 16) return false;
+  // largest (row-part elements x holes) product must fit the pair table
+  const int na = h->L - h->split;
+  if ((na / 2) * (na - na / 2) > kMaxIntraRow) return false;
+  return static_cast<size_t>(h->max_row) * elem <= 160 * 1024;
+}
+
 unsigned grid_for(uint64_t n) {
   uint64_t g = (n + kThreads - 1) / kThreads;
   const uint64_t cap = static_cast<uint64_t>(device_sm_count()) * 8;
@@ -173,9 +328,13 @@ unsigned grid_for(uint64_t n) {
 }  // namespace
 
 int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t st) {
-  if (precision == DOCI_FP64) return launch_typed<double>(h, x, y, st);
-  if (precision == DOCI_FP32) return launch_typed<float>(h, x, y, st);
-  return DOCI_ERR_INVALID;
+  if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
+  const size_t elem = precision == DOCI_FP64 ? 8 : 4;
+  // row kernel when the row tiling exists, fits, and gives every SM work
+  bool row = h->sigma_kernel == 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
+  if (row && !row_kernel_fits(h, elem)) row = false;
+  if (precision == DOCI_FP64) return row ? launch_row<double>(h, x, y, st) : launch_typed<double>(h, x, y, st);
+  return row ? launch_row<float>(h, x, y, st) : launch_typed<float>(h, x, y, st);
 }
 
 int launch_diagonal(doci_ham *h, cudaStream_t st) {

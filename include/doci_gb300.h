@@ -139,6 +139,11 @@ const double *doci_ham_diagonal_device(const doci_ham *ham);
  * stream (NULL = the handle's stream). */
 int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *stream);
 
+/* Sigma kernel selection for a handle: 0 automatic (default), 1 the
+ * per-determinant gather kernel, 2 the row-tiled kernel (falls back to 1
+ * when the handle has no row tiling).  For tests and tuning. */
+int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
+
 /* Same on host buffers; copies in and out inside the call, synchronous. */
 int doci_sigma_host(doci_ham *ham, const void *x, void *y, int precision);
 

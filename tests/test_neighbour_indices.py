@@ -10,6 +10,7 @@ import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "host_checks", "neighbours_check.cu")
+ROW_SRC = os.path.join(HERE, "host_checks", "row_check.cu")
 
 
 @pytest.fixture(scope="module")
@@ -29,5 +30,27 @@ def exe(tmp_path_factory):
 ])
 def test_neighbour_ranks(exe, L, N, stride):
     r = subprocess.run([exe, str(L), str(N), str(stride)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad=0" in r.stdout
+
+
+@pytest.fixture(scope="module")
+def row_exe(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    out = str(tmp_path_factory.mktemp("rowc") / "row_check")
+    subprocess.run([nvcc, "-O2", "-std=c++17", ROW_SRC, "-o", out], check=True)
+    return out
+
+
+@pytest.mark.parametrize("L,N,split,rs,cs", [
+    (10, 5, 6, 1, 1), (12, 6, 8, 1, 1), (12, 3, 8, 1, 1), (12, 9, 8, 1, 1), (14, 7, 9, 1, 1),
+    (16, 8, 10, 1, 1), (18, 9, 9, 1, 1), (20, 10, 9, 3, 5), (24, 12, 13, 7, 11), (28, 14, 16, 37, 101),
+    (32, 16, 16, 257, 1009), (32, 2, 16, 1, 1), (32, 30, 16, 1, 1), (28, 7, 16, 5, 17), (9, 0, 8, 1, 1),
+    (9, 9, 8, 1, 1), (17, 1, 16, 1, 1), (17, 16, 16, 1, 1),
+])
+def test_row_kernel_ranks(row_exe, L, N, split, rs, cs):
+    r = subprocess.run([row_exe, str(L), str(N), str(split), str(rs), str(cs)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad=0" in r.stdout

@@ -50,12 +50,15 @@ def test_golden_sigma_diag_bits(name, fcidump, dg):
         assert np.array_equal(ranks.cpu().numpy(), np.arange(h.D))
 
 
+@pytest.mark.parametrize("kernel", ["gather", "row"])
 @pytest.mark.parametrize("L,N,seed", [(16, 8, 21), (18, 5, 22), (20, 10, 23), (12, 1, 24), (12, 11, 25),
-                                      (7, 0, 26), (6, 6, 27), (32, 2, 28), (32, 30, 29), (24, 12, 30)])
-def test_sigma_vs_oracle(L, N, seed, synth, dg):
+                                      (7, 0, 26), (6, 6, 27), (32, 2, 28), (32, 30, 29), (24, 12, 30),
+                                      (22, 11, 31), (26, 4, 32)])
+def test_sigma_vs_oracle(L, N, seed, kernel, synth, dg):
     p = synth(L, N, seed)
     o = oracle.Ham(p)
     with dg.Hamiltonian.from_fcidump(p) as h:
+        h.set_sigma_kernel(kernel)
         assert h.D == o.D
         assert np.array_equal(h.diagonal(), o.diag)
         x = np.random.default_rng(seed).standard_normal(h.D)
@@ -88,13 +91,15 @@ def test_addressing_full_size_properties(synth, dg):
             assert all(bin(int(v)).count("1") == 16 for v in b[:64])
 
 
-def test_sigma_full_size_symmetry_and_linearity(synth, dg):
+@pytest.mark.parametrize("kernel", ["gather", "row"])
+def test_sigma_full_size_symmetry_and_linearity(kernel, synth, dg):
     """L=28, N=14 (D = 40,116,600): H is symmetric, sigma is linear, and
     sampled rows agree with the oracle's gather form."""
     torch = torch_cuda()
     p = synth(28, 14, 2)
     o = oracle.Ham(p, keep_diag=False)
     with dg.Hamiltonian.from_fcidump(p) as h:
+        h.set_sigma_kernel(kernel)
         D = h.D
         g = torch.Generator(device="cuda").manual_seed(7)
         x = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
@@ -119,3 +124,32 @@ def test_sigma_full_size_symmetry_and_linearity(synth, dg):
         ref = o.gather_rows(xs, first, length, dg_rows)
         got = hx.cpu().numpy()[rows]
         assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_row_and_gather_kernels_agree_at_L32(synth, dg):
+    """L=32, N=16 (D = 601,080,390), FP32: the two sigma kernels agree
+    (different summation orders: FP32 tolerance), and sampled rows agree with
+    the FP64 oracle gather form."""
+    torch = torch_cuda()
+    p = synth(32, 16, 3)
+    o = oracle.Ham(p, keep_diag=False)
+    with dg.Hamiltonian.from_fcidump(p) as h:
+        D = h.D
+        g = torch.Generator(device="cuda").manual_seed(3)
+        x = torch.randn(D, dtype=torch.float32, device="cuda", generator=g)
+        ya = torch.empty_like(x)
+        yb = torch.empty_like(x)
+        h.set_sigma_kernel("gather")
+        h.sigma_device(x.data_ptr(), ya.data_ptr(), dg.FP32)
+        h.set_sigma_kernel("row")
+        h.sigma_device(x.data_ptr(), yb.data_ptr(), dg.FP32)
+        torch.cuda.synchronize()
+        scale = ya.abs().max().item()
+        assert (ya - yb).abs().max().item() <= 2e-6 * scale
+        first = np.array([0, 250_000_000, D - 2000], dtype=np.uint64)
+        length = np.array([2000, 2000, 2000], dtype=np.uint64)
+        rows = np.concatenate([np.arange(f, f + n) for f, n in zip(first, length)]).astype(np.int64)
+        xs = x.double().cpu().numpy()
+        ref = o.gather_rows(xs, first, length, h.diagonal()[rows])
+        got = yb.cpu().numpy()[rows]
+        assert np.abs(got - ref).max() <= 2e-6 * np.abs(ref).max()
