@@ -42,9 +42,9 @@ bool reg_has(const void *h) {
   return g_live.count(h) != 0;
 }
 
-cudaStream_t pick(doci_ham *h, void *stream) {
-  return stream ? static_cast<cudaStream_t>(stream) : h->stream;
-}
+// Streams are used as given, as everywhere in CUDA: NULL is the default
+// stream, so work queued by the caller on it is ordered before ours.
+cudaStream_t pick(doci_ham *, void *stream) { return static_cast<cudaStream_t>(stream); }
 
 struct DevBuf {
   void *p = nullptr;

@@ -14,8 +14,9 @@
  * Part 2 is the status-returning API: device Hamiltonian handles, sigma on
  * device or host buffers, the device-resident solvers (FP64 and mixed
  * FP32/FP64), batched solves and the request server.  Every call returns a
- * doci_status; none exits.  Streams are passed as void* (a cudaStream_t, or
- * NULL for the handle's own stream).  No CUDA or torch types appear here.
+ * doci_status; none exits.  Streams are passed as void* (a cudaStream_t;
+ * NULL is CUDA's default stream, as in the CUDA API itself).  No CUDA or
+ * torch types appear here.
  */
 #ifndef DOCI_GB300_H
 #define DOCI_GB300_H
@@ -136,7 +137,7 @@ const double *doci_ham_diagonal_device(const doci_ham *ham);
 
 /* sigma = H x on device buffers of D elements (double for DOCI_FP64, float
  * for DOCI_FP32).  y is overwritten; x and y must not alias.  Asynchronous on
- * stream (NULL = the handle's stream). */
+ * stream (NULL = the default stream). */
 int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *stream);
 
 /* Sigma kernel selection for a handle: 0 automatic (default), 1 the
