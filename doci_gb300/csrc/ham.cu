@@ -52,7 +52,13 @@ void ham_release(doci_ham *h) {
   cudaFree(h->d_stage_y);
   cudaFree(h->d_rows);
   cudaFree(h->d_rowstart);
-  h->d_rows = h->d_rowstart = nullptr;
+  cudaFree(h->d_sector_rs);
+  cudaFree(h->d_sector_off);
+  cudaFree(h->d_panels[0]);
+  cudaFree(h->d_panels[1]);
+  h->d_panels[0] = h->d_panels[1] = nullptr;
+  h->d_sector_off = nullptr;
+  h->d_rows = h->d_rowstart = h->d_sector_rs = nullptr;
   if (h->h_diag) cudaFreeHost(h->h_diag);
   if (h->stream) cudaStreamDestroy(h->stream);
   h->d_binom = nullptr;
@@ -198,10 +204,48 @@ int ham_build_rows(doci_ham *h) {
   }
   h->nrows = static_cast<int>(order.size());
   h->max_row = max_row;
+  // sector lists: sector k holds the row-part sets with k elements; the set
+  // with colex rank g sits at index C(na, k) - 1 - g
+  std::vector<uint32_t> sector(size_t(1) << na, 0xffffffffu);
+  int off = 0, max_sector = 0;
+  for (int k = 0; k <= na; ++k) {
+    h->sector_off[k] = off;
+    const int cnt = static_cast<int>(binom64(na, k));
+    if (N - k >= 0 && N - k <= split && cnt > max_sector) max_sector = cnt;
+    off += cnt;
+  }
+  h->sector_off[na + 1] = off;
+  for (uint32_t mask = 0; mask < (1u << na); ++mask) {
+    const int k = __builtin_popcount(mask);
+    uint64_t colex = 0;
+    for (int a = 0, t = 0; a < na; ++a)
+      if (mask >> a & 1u) colex += binom64(a, ++t);
+    sector[h->sector_off[k] + (binom64(na, k) - 1 - colex)] = start[mask];
+  }
+  h->max_sector_rows = max_sector;
   DOCI_CUDA(cudaMalloc(&h->d_rows, rows.size() * sizeof(uint32_t)));
   DOCI_CUDA(cudaMalloc(&h->d_rowstart, start.size() * sizeof(uint32_t)));
   DOCI_CUDA(cudaMemcpyAsync(h->d_rows, rows.data(), rows.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_rowstart, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                            h->stream));
+  DOCI_CUDA(cudaMalloc(&h->d_sector_off, sizeof(h->sector_off)));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_sector_off, h->sector_off, sizeof(h->sector_off), cudaMemcpyHostToDevice, h->stream));
+  for (int v = 0; v < 2; ++v) {  // column panels of 2 (FP64) or 4 (FP32) columns
+    const int W = v == 0 ? 2 : 4;
+    std::vector<int2> pv;
+    for (int k = 0; k <= na; ++k) {
+      const int j = N - k;
+      if (j < 0 || j > split) continue;
+      const uint64_t ncol = binom64(split, j);
+      for (uint64_t c0 = 0; c0 < ncol; c0 += W) pv.push_back(make_int2(k, static_cast<int>(c0)));
+    }
+    h->npanels[v] = static_cast<int>(pv.size());
+    DOCI_CUDA(cudaMalloc(&h->d_panels[v], pv.size() * sizeof(int2)));
+    DOCI_CUDA(cudaMemcpyAsync(h->d_panels[v], pv.data(), pv.size() * sizeof(int2), cudaMemcpyHostToDevice, h->stream));
+    DOCI_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  DOCI_CUDA(cudaMalloc(&h->d_sector_rs, sector.size() * sizeof(uint32_t)));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_sector_rs, sector.data(), sector.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                             h->stream));
   DOCI_CUDA(cudaStreamSynchronize(h->stream));
   return DOCI_OK;

@@ -84,6 +84,14 @@ struct doci_ham {
   uint32_t *d_rows = nullptr;     // nrows x {rowstart, mask | k << 24}
   int sigma_kernel = 0;           // 0 automatic, 1 per-determinant gather, 2 row kernel
   uint32_t *d_rowstart = nullptr; // 2^(L - split) entries: row start by row-part mask
+  // column-panel pass (row-part hops): rows of each sector (fixed |row part|)
+  // listed by reversed colex of the row-part set
+  uint32_t *d_sector_rs = nullptr; // sum_k C(L - split, k) row starts
+  int sector_off[33] = {};         // offset of sector k in d_sector_rs
+  int max_sector_rows = 0;
+  int *d_sector_off = nullptr;     // sector_off on the device
+  int2 *d_panels[2] = {};          // column panels {k, c0}: [0] FP64 (2 columns), [1] FP32 (4 columns)
+  int npanels[2] = {};
 
   // host diagonal for doci_get_diagonal (lazy)
   double *h_diag = nullptr;

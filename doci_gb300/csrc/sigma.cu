@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <type_traits>
+#include <vector>
 
 #include "addressing.cuh"
 #include "internal.h"
@@ -205,8 +206,8 @@ struct RowTables {
 };
 
 template <typename Real, int NHB>
-__global__ void __launch_bounds__(kRowThreads)
-sigma_row_kernel(RowShape s, const uint2 *__restrict__ rows, const uint32_t *__restrict__ rowstart_of,
+__global__ void __launch_bounds__(kRowThreads, 3)
+sigma_row_kernel(RowShape s, int with_across, const uint2 *__restrict__ rows, const uint32_t *__restrict__ rowstart_of,
                  const uint32_t *__restrict__ g_binom, const Real *__restrict__ g_K, const Real *__restrict__ diag,
                  const Real *__restrict__ x, Real *__restrict__ y) {
   __shared__ RowTables<Real> tb;
@@ -244,10 +245,10 @@ sigma_row_kernel(RowShape s, const uint2 *__restrict__ rows, const uint32_t *__r
       if (lane == 0) {
         tb.n_ab = j < sp ? ne : 0;   // a column-part hole must exist
         tb.n_ba = j > 0 ? nhl : 0;   // a column-part element must exist
-        tb.n_aa = ne * nhl;
+        tb.n_aa = with_across ? ne * nhl : 0;
       }
       // row part -> row part pairs (element e, hole h)
-      for (int t = lane; t < ne * nhl; t += 32) {
+      for (int t = lane; with_across && t < ne * nhl; t += 32) {
         const int e = t / nhl, h = t % nhl;
         const int a_e = __fns(eb, 0, e + 1), a_h = __fns(hb, 0, h + 1);
         tb.aa_rs[t] = rowstart_of[(mask & ~(1u << a_e)) | (1u << a_h)];
@@ -283,7 +284,7 @@ sigma_row_kernel(RowShape s, const uint2 *__restrict__ rows, const uint32_t *__r
 }
 
 template <typename Real>
-int launch_row(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
+int launch_row(const doci_ham *h, const void *x, void *y, cudaStream_t st, int with_across) {
   const RowShape s{h->D, h->L, h->N, h->split, h->L - h->split, h->nrows};
   const size_t dyn = static_cast<size_t>(h->max_row) * sizeof(Real);
   auto kern = sigma_row_kernel<Real, 16>;
@@ -302,8 +303,8 @@ int launch_row(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
                                                    : reinterpret_cast<const Real *>(h->d_Kmir32);
   const Real *dg = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_diag)
                                                     : reinterpret_cast<const Real *>(h->d_diag32);
-  kern<<<grid, kRowThreads, dyn, st>>>(s, reinterpret_cast<const uint2 *>(h->d_rows), h->d_rowstart, h->d_binom, K,
-                                       dg, static_cast<const Real *>(x), static_cast<Real *>(y));
+  kern<<<grid, kRowThreads, dyn, st>>>(s, with_across, reinterpret_cast<const uint2 *>(h->d_rows), h->d_rowstart,
+                                       h->d_binom, K, dg, static_cast<const Real *>(x), static_cast<Real *>(y));
   DOCI_CUDA(cudaGetLastError());
   return DOCI_OK;
 }
@@ -316,6 +317,122 @@ bool row_kernel_fits(const doci_ham *h, size_t elem) {
   const int na = h->L - h->split;
   if ((na / 2) * (na - na / 2) > kMaxIntraRow) return false;
   return static_cast<size_t>(h->max_row) * elem <= 160 * 1024;
+}
+
+// ---------------------------------------------------------------------------
+// Column-panel pass: the row-part hops (both orbitals in the row part) keep
+// the column and change the row, within one sector (rows with the same
+// number k of row-part elements).  One block loads W consecutive columns of
+// every row of a sector into shared memory (panel[row][w]), so each x element
+// is read once per pass, and each thread gathers its row's k (na - k)
+// neighbour rows from the panel, W columns per load.  Sector-local row index
+// = C(na, k) - 1 - colex of the row-part set, so the neighbour machinery of
+// addressing.cuh gives neighbour indices directly.  Adds into y (the row
+// pass has written diagonal, column-part and cross hops).
+// ---------------------------------------------------------------------------
+constexpr int kColThreads = 256;
+
+struct ColShape {
+  int L, N, split, na;
+};
+
+template <typename Real, int W>
+struct Vec;
+template <>
+struct Vec<float, 4> {
+  using T = float4;
+};
+template <>
+struct Vec<double, 2> {
+  using T = double2;
+};
+
+template <typename Real, int W, int NHA>
+__global__ void __launch_bounds__(kColThreads)
+sigma_col_kernel(ColShape s, const int2 *__restrict__ panels, int npanels, const uint32_t *__restrict__ sector_rs,
+                 const int *__restrict__ sector_off, const uint32_t *__restrict__ g_binom,
+                 const Real *__restrict__ g_K, const Real *__restrict__ x, Real *__restrict__ y) {
+  __shared__ uint32_t binom[kBinomRows * kBinomCols];
+  __shared__ Real K[32 * 32];
+  extern __shared__ __align__(16) unsigned char col_smem[];
+  Real *P = reinterpret_cast<Real *>(col_smem);
+  for (int t = threadIdx.x; t < kBinomRows * kBinomCols; t += blockDim.x) binom[t] = g_binom[t];
+  for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) K[t] = g_K[t];
+  const int sp = s.split, na = s.na;
+  for (int pi = blockIdx.x; pi < npanels; pi += gridDim.x) {
+    const int2 pn = panels[pi];
+    const int k = pn.x, j = s.N - k;
+    const uint32_t c0 = static_cast<uint32_t>(pn.y);
+    __syncthreads();
+    const uint32_t ncol = binom[sp * kBinomCols + j];
+    const uint32_t wc = ncol - c0 < static_cast<uint32_t>(W) ? ncol - c0 : static_cast<uint32_t>(W);
+    const uint32_t nr = binom[na * kBinomCols + k];
+    const uint32_t *rs = sector_rs + sector_off[k];
+    for (uint32_t t = threadIdx.x; t < nr * W; t += blockDim.x) {
+      const uint32_t r = t / W, w = t % W;
+      P[t] = w < wc ? x[rs[r] + c0 + w] : Real(0);
+    }
+    __syncthreads();
+    const Real *Kbase = K + sp * 32 + sp;
+    for (uint32_t r = threadIdx.x; r < nr; r += blockDim.x) {
+      const uint32_t R = nr - 1 - r;
+      const uint32_t M = dev::colex_unrank<kBinomCols>(R, na, k, binom);
+      dev::Neighbours<NHA, kBinomCols> nb;
+      nb.precompute(M, R, na, na - k, binom);
+      struct Acc {
+        const Real *Kb, *P;
+        const Real *Krow;
+        Real a[W];
+        __device__ __forceinline__ void begin(int m) { Krow = Kb + m * 32; }
+        __device__ __forceinline__ void hop(int, int q, uint32_t idx) {
+          const typename Vec<Real, W>::T v = *reinterpret_cast<const typename Vec<Real, W>::T *>(P + idx * W);
+          const Real kv = Krow[q];
+          const Real *vv = reinterpret_cast<const Real *>(&v);
+#pragma unroll
+          for (int w = 0; w < W; ++w) a[w] += kv * vv[w];
+        }
+      } f{Kbase, P, Kbase, {}};
+      nb.visit(M, R, nr - 1, k, na - k, binom, f);
+      Real *yo = y + rs[r] + c0;
+#pragma unroll
+      for (int w = 0; w < W; ++w)
+        if (static_cast<uint32_t>(w) < wc) yo[w] += f.a[w];
+    }
+  }
+}
+
+template <typename Real>
+int launch_col(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
+  constexpr int W = sizeof(Real) == 4 ? 4 : 2;
+  const ColShape s{h->L, h->N, h->split, h->L - h->split};
+  const int v = sizeof(Real) == 4 ? 1 : 0;
+  const int2 *d_panels = h->d_panels[v];
+  const int npanels = h->npanels[v];
+  const size_t dyn = static_cast<size_t>(h->max_sector_rows) * W * sizeof(Real);
+  auto kern = sigma_col_kernel<Real, W, 16>;
+  static size_t configured = 0;
+  static int blocks_per_sm = 1;
+  if (configured != dyn) {
+    DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kColThreads, dyn);
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    configured = dyn;
+  }
+  int grid = device_sm_count() * blocks_per_sm;
+  if (grid > npanels) grid = npanels;
+  const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
+                                                   : reinterpret_cast<const Real *>(h->d_Kmir32);
+  kern<<<grid, kColThreads, dyn, st>>>(s, d_panels, npanels, h->d_sector_rs, h->d_sector_off, h->d_binom, K,
+                                       static_cast<const Real *>(x), static_cast<Real *>(y));
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+bool col_pass_fits(const doci_ham *h, size_t elem) {
+  const int W = elem == 4 ? 4 : 2;
+  const int na = h->L - h->split;
+  if (na < 1 || na > 32 || na - 0 > 24) return false;
+  return static_cast<size_t>(h->max_sector_rows) * W * elem <= 210 * 1024;
 }
 
 unsigned grid_for(uint64_t n) {
@@ -331,10 +448,15 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
   if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
   const size_t elem = precision == DOCI_FP64 ? 8 : 4;
   // row kernel when the row tiling exists, fits, and gives every SM work
-  bool row = h->sigma_kernel == 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
+  bool row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
-  if (precision == DOCI_FP64) return row ? launch_row<double>(h, x, y, st) : launch_typed<double>(h, x, y, st);
-  return row ? launch_row<float>(h, x, y, st) : launch_typed<float>(h, x, y, st);
+  if (!row) return precision == DOCI_FP64 ? launch_typed<double>(h, x, y, st) : launch_typed<float>(h, x, y, st);
+  // row-part hops in a column-panel pass when its panel fits shared memory
+  const bool col = h->sigma_kernel != 3 && col_pass_fits(h, elem);
+  int r = precision == DOCI_FP64 ? launch_row<double>(h, x, y, st, col ? 0 : 1)
+                                 : launch_row<float>(h, x, y, st, col ? 0 : 1);
+  if (r || !col) return r;
+  return precision == DOCI_FP64 ? launch_col<double>(h, x, y, st) : launch_col<float>(h, x, y, st);
 }
 
 int launch_diagonal(doci_ham *h, cudaStream_t st) {

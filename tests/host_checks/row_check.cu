@@ -133,6 +133,44 @@ int main(int argc, char **argv) {
     }
   }
   if (covered != x.D) ++bad;
+  // Column-panel pass: sector-local row index = C(na,k) - 1 - colex(R); the
+  // neighbour machinery on the row part must give the index of R \ m u q,
+  // and every row-part hop of R exactly once.
+  long col_rows = 0;
+  for (uint32_t R = 0; R < (1u << na); R += static_cast<uint32_t>(rstride)) {
+    if (!row_valid(x, R)) continue;
+    const int k = __builtin_popcount(R);
+    const uint32_t nr = static_cast<uint32_t>(binom(na, k));
+    uint32_t colex = 0;
+    for (int a = 0, t = 0; a < na; ++a)
+      if (R >> a & 1u) colex += static_cast<uint32_t>(binom(a, ++t));
+    struct ColCheck {
+      uint32_t R;
+      int na, k;
+      uint32_t nr;
+      long bad = 0, hops = 0;
+      std::vector<char> seen = std::vector<char>(64 * 64, 0);
+      void begin(int) {}
+      void hop(int m, int q, uint32_t idx) {
+        ++hops;
+        if (!(R >> m & 1u) || (R >> q & 1u) || idx >= nr || seen[m * 64 + q]++) { ++bad; return; }
+        const uint32_t R2 = (R & ~(1u << m)) | (1u << q);
+        uint32_t c2 = 0;
+        for (int a = 0, t = 0; a < na; ++a)
+          if (R2 >> a & 1u) c2 += static_cast<uint32_t>(binom(a, ++t));
+        if (idx != nr - 1 - c2) ++bad;
+      }
+    } f{R, na, k, nr};
+    const uint32_t M = doci::dev::colex_unrank<BC>(colex, na, k, x.B.data());
+    if (M != R) ++bad;
+    doci::dev::Neighbours<16, BC> nb;
+    nb.precompute(M, colex, na, na - k, x.B.data());
+    nb.visit(M, colex, nr - 1, k, na - k, x.B.data(), f);
+    if (f.hops != static_cast<long>(k) * (na - k)) ++bad;
+    bad += f.bad;
+    ++col_rows;
+  }
+  std::printf("column pass rows checked=%ld\n", col_rows);
   std::printf("L=%d N=%d split=%d rows=%ld dets=%ld bad=%ld\n", x.L, x.N, x.sp, rows, dets, bad);
   return bad ? 1 : 0;
 }
