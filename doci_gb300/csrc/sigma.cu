@@ -409,16 +409,19 @@ int launch_col(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
   const int2 *d_panels = h->d_panels[v];
   const int npanels = h->npanels[v];
   const size_t dyn = static_cast<size_t>(h->max_sector_rows) * W * sizeof(Real);
-  auto kern = sigma_col_kernel<Real, W, 16>;
-  static size_t configured = 0;
-  static int blocks_per_sm = 1;
-  if (configured != dyn) {
+  // the neighbour routine keeps one register slot per row-part hole
+  const int kmin = h->N - h->split > 0 ? h->N - h->split : 0;
+  const bool wide = s.na - kmin > 16;
+  auto kern = wide ? sigma_col_kernel<Real, W, 24> : sigma_col_kernel<Real, W, 16>;
+  static size_t configured[2] = {0, 0};
+  static int blocks_per_sm[2] = {1, 1};
+  if (configured[wide] != dyn) {
     DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kColThreads, dyn);
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
-    configured = dyn;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[wide], kern, kColThreads, dyn);
+    if (blocks_per_sm[wide] < 1) blocks_per_sm[wide] = 1;
+    configured[wide] = dyn;
   }
-  int grid = device_sm_count() * blocks_per_sm;
+  int grid = device_sm_count() * blocks_per_sm[wide];
   if (grid > npanels) grid = npanels;
   const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
                                                    : reinterpret_cast<const Real *>(h->d_Kmir32);

@@ -163,9 +163,17 @@ int main(int argc, char **argv) {
     } f{R, na, k, nr};
     const uint32_t M = doci::dev::colex_unrank<BC>(colex, na, k, x.B.data());
     if (M != R) ++bad;
-    doci::dev::Neighbours<16, BC> nb;
-    nb.precompute(M, colex, na, na - k, x.B.data());
-    nb.visit(M, colex, nr - 1, k, na - k, x.B.data(), f);
+    // same register bound as the library: 16 row-part holes, else 24
+    const int kmin = x.N - x.sp > 0 ? x.N - x.sp : 0;
+    if (na - kmin > 16) {
+      doci::dev::Neighbours<24, BC> nb;
+      nb.precompute(M, colex, na, na - k, x.B.data());
+      nb.visit(M, colex, nr - 1, k, na - k, x.B.data(), f);
+    } else {
+      doci::dev::Neighbours<16, BC> nb;
+      nb.precompute(M, colex, na, na - k, x.B.data());
+      nb.visit(M, colex, nr - 1, k, na - k, x.B.data(), f);
+    }
     if (f.hops != static_cast<long>(k) * (na - k)) ++bad;
     bad += f.bad;
     ++col_rows;

@@ -49,6 +49,9 @@ def row_exe(tmp_path_factory):
     (16, 8, 10, 1, 1), (18, 9, 9, 1, 1), (20, 10, 9, 3, 5), (24, 12, 13, 7, 11), (28, 14, 16, 37, 101),
     (32, 16, 16, 257, 1009), (32, 2, 16, 1, 1), (32, 30, 16, 1, 1), (28, 7, 16, 5, 17), (9, 0, 8, 1, 1),
     (9, 9, 8, 1, 1), (17, 1, 16, 1, 1), (17, 16, 16, 1, 1),
+    # the splits the library picks for small-N / large-N spaces (row part up to 24 orbitals)
+    (32, 2, 8, 1, 1), (32, 30, 8, 1, 1), (32, 3, 8, 3, 1), (26, 4, 8, 1, 1), (24, 12, 13, 7, 11),
+    (26, 4, 12, 1, 1), (22, 11, 11, 1, 7), (20, 10, 9, 1, 3),
 ])
 def test_row_kernel_ranks(row_exe, L, N, split, rs, cs):
     r = subprocess.run([row_exe, str(L), str(N), str(split), str(rs), str(cs)], capture_output=True, text=True)
