@@ -197,54 +197,5 @@ DOCI_HD void row_column_hops(uint32_t c, uint32_t n, int sp, int j, const uint32
   for (int t = 0; t < n_aa; ++t) f.across(t, c);
 }
 
-// Same traversal as row_column_hops, with the cross and row-part hops handed
-// over as whole groups (f.down_all(n_ba, c'), f.up_all(n_ab, q, c'),
-// f.across_all(n_aa, c)) so the caller can issue their loads together.
-template <int NHB, int BC, typename F>
-DOCI_HD void row_column_hops_grouped(uint32_t c, uint32_t n, int sp, int j, const uint32_t *B, int n_ab, int n_ba,
-                                     int n_aa, F &f) {
-  const uint32_t p = n - 1 - c;
-  const uint32_t Mb = colex_unrank<BC>(p, sp, j, B);
-  Neighbours<NHB, BC> nb;
-  nb.precompute(Mb, p, sp, sp - j, B);
-  const int nhB = sp - j;
-  const uint32_t n_up_m1 = (j < sp ? B[sp * BC + j + 1] : 1u) - 1u;
-  const uint32_t n_dn_m1 = (j > 0 ? B[sp * BC + j - 1] : 1u) - 1u;
-  uint32_t PVtot = 0, PUtot = 0;
-  {
-    uint32_t mr = Mb;
-    for (int i = 0; i < j; ++i) {
-      const int m = ffs32(mr) - 1;
-      mr &= mr - 1;
-      PVtot += B[m * BC + i + 2];
-      PUtot += B[m * BC + i];
-    }
-  }
-  uint32_t mrem = Mb, PW = 0, PU = 0, PV = 0;
-  for (int kk = 0; kk < j; ++kk) {
-    const int m = ffs32(mrem) - 1;
-    mrem &= mrem - 1;
-    const uint32_t W = B[m * BC + kk + 1], U = B[m * BC + kk], V = B[m * BC + kk + 2];
-    const uint32_t base1 = n - 1 - (PV + p - (PW + W));
-    const uint32_t base2 = n - 1 - (PW - (PU + U));
-    f.begin(m);
-#pragma unroll
-    for (int h = 0; h < NHB; ++h) {
-      if (h < nhB) f.inrow(m, nb.Q[h], nb.Q[h] < m ? base1 - nb.E1[h] : base2 - nb.E2[h]);
-    }
-    if (n_ba > 0) f.down_all(n_ba, n_dn_m1 - (PW + PUtot - (PU + U)));
-    PW += W;
-    PU += U;
-    PV += V;
-  }
-  if (n_ab > 0) {
-#pragma unroll
-    for (int h = 0; h < NHB; ++h) {
-      if (h < nhB) f.up_all(n_ab, nb.Q[h], n_up_m1 - (nb.E1[h] + PVtot));
-    }
-  }
-  if (n_aa > 0) f.across_all(n_aa, c);
-}
-
 }  // namespace dev
 }  // namespace doci

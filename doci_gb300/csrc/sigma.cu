@@ -264,44 +264,21 @@ sigma_row_kernel(RowShape s, int with_across, const uint2 *__restrict__ rows, co
       const RowTables<Real> &tb;
       const Real *xs, *x;
       const Real *Krow;
-      Real acc, acc2;
+      Real acc;
       __device__ __forceinline__ void begin(int m) { Krow = tb.K + m * 32; }
       __device__ __forceinline__ void inrow(int, int q, uint32_t cc) { acc += Krow[q] * xs[cc]; }
-      // the cross-hop loops issue their independent loads four at a time
-      __device__ __forceinline__ void down_all(int n_ba, uint32_t cc) {
-        int t = 0;
-        for (; t + 4 <= n_ba; t += 4) {
-          const Real v0 = __ldg(x + tb.ba_rs[t] + cc), v1 = __ldg(x + tb.ba_rs[t + 1] + cc);
-          const Real v2 = __ldg(x + tb.ba_rs[t + 2] + cc), v3 = __ldg(x + tb.ba_rs[t + 3] + cc);
-          acc2 += Krow[tb.ba_q[t]] * v0 + Krow[tb.ba_q[t + 1]] * v1 + Krow[tb.ba_q[t + 2]] * v2 +
-                  Krow[tb.ba_q[t + 3]] * v3;
-        }
-        for (; t < n_ba; ++t) acc2 += Krow[tb.ba_q[t]] * __ldg(x + tb.ba_rs[t] + cc);
+      __device__ __forceinline__ void down(int t, int, int q, uint32_t cc) {
+        acc += Krow[q] * __ldg(x + tb.ba_rs[t] + cc);
       }
-      __device__ __forceinline__ void up_all(int n_ab, int q, uint32_t cc) {
-        int t = 0;
-        for (; t + 4 <= n_ab; t += 4) {
-          const Real v0 = __ldg(x + tb.ab_rs[t] + cc), v1 = __ldg(x + tb.ab_rs[t + 1] + cc);
-          const Real v2 = __ldg(x + tb.ab_rs[t + 2] + cc), v3 = __ldg(x + tb.ab_rs[t + 3] + cc);
-          acc2 += tb.K[tb.ab_m[t] * 32 + q] * v0 + tb.K[tb.ab_m[t + 1] * 32 + q] * v1 +
-                  tb.K[tb.ab_m[t + 2] * 32 + q] * v2 + tb.K[tb.ab_m[t + 3] * 32 + q] * v3;
-        }
-        for (; t < n_ab; ++t) acc2 += tb.K[tb.ab_m[t] * 32 + q] * __ldg(x + tb.ab_rs[t] + cc);
+      __device__ __forceinline__ void up(int t, int m, int q, uint32_t cc) {
+        acc += tb.K[m * 32 + q] * __ldg(x + tb.ab_rs[t] + cc);
       }
-      __device__ __forceinline__ void across_all(int n_aa, uint32_t cc) {
-        int t = 0;
-        for (; t + 4 <= n_aa; t += 4) {
-          const Real v0 = __ldg(x + tb.aa_rs[t] + cc), v1 = __ldg(x + tb.aa_rs[t + 1] + cc);
-          const Real v2 = __ldg(x + tb.aa_rs[t + 2] + cc), v3 = __ldg(x + tb.aa_rs[t + 3] + cc);
-          acc += tb.aa_K[t] * v0 + tb.aa_K[t + 1] * v1 + tb.aa_K[t + 2] * v2 + tb.aa_K[t + 3] * v3;
-        }
-        for (; t < n_aa; ++t) acc += tb.aa_K[t] * __ldg(x + tb.aa_rs[t] + cc);
-      }
+      __device__ __forceinline__ void across(int t, uint32_t cc) { acc += tb.aa_K[t] * __ldg(x + tb.aa_rs[t] + cc); }
     };
     for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) {
-      Acc f{tb, xs, x, tb.K, diag[rstart + c] * xs[c], Real(0)};
-      dev::row_column_hops_grouped<NHB, kBinomCols>(c, n, sp, j, B, n_ab, n_ba, n_aa, f);
-      y[rstart + c] = f.acc + f.acc2;
+      Acc f{tb, xs, x, tb.K, diag[rstart + c] * xs[c]};
+      dev::row_column_hops<NHB, kBinomCols>(c, n, sp, j, B, n_ab, tb.ab_m, n_ba, tb.ba_q, n_aa, f);
+      y[rstart + c] = f.acc;
     }
   }
 }

@@ -67,21 +67,6 @@ struct Check {
   void up(int t, int m, int q, uint32_t c) { visit(m, q, ab_rs[t] + c, c, ab_len[t]); }
   void down(int t, int m, int q, uint32_t c) { visit(m, q, ba_rs[t] + c, c, ba_len[t]); }
   void across(int t, uint32_t c) { visit(aa_m[t], aa_q[t], aa_rs[t] + c, c, n); }
-  // grouped traversal (row_column_hops_grouped)
-  int cur_m = -1;
-  const int *ab_m_tab = nullptr, *ba_q_tab = nullptr;
-  void down_all(int n_ba, uint32_t c) {
-    for (int t = 0; t < n_ba; ++t) down(t, cur_m, ba_q_tab[t], c);
-  }
-  void up_all(int n_ab, int q, uint32_t c) {
-    for (int t = 0; t < n_ab; ++t) up(t, ab_m_tab[t], q, c);
-  }
-  void across_all(int n_aa, uint32_t c) {
-    for (int t = 0; t < n_aa; ++t) across(t, c);
-  }
-};
-struct GroupedCheck : Check {
-  void begin(int m) { cur_m = m; }
 };
 
 int main(int argc, char **argv) {
@@ -144,14 +129,6 @@ int main(int argc, char **argv) {
                                          static_cast<int>(aa_rs.size()), f);
       if (f.hops != static_cast<long>(x.N) * (x.L - x.N)) ++bad;
       bad += f.bad;
-      GroupedCheck g{{x, T, rs, n, ab_rs.data(), ba_rs.data(), aa_rs.data(), aa_m.data(), aa_q.data(), ab_len.data(),
-                      ba_len.data()}};
-      g.ab_m_tab = ab_m.data();
-      g.ba_q_tab = ba_q.data();
-      doci::dev::row_column_hops_grouped<16, BC>(c, n, x.sp, j, x.B.data(), n_ab, n_ba,
-                                                 static_cast<int>(aa_rs.size()), g);
-      if (g.hops != static_cast<long>(x.N) * (x.L - x.N)) ++bad;
-      bad += g.bad;
       ++dets;
     }
   }
