@@ -454,8 +454,9 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
   bool row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
   if (!row) return precision == DOCI_FP64 ? launch_typed<double>(h, x, y, st) : launch_typed<float>(h, x, y, st);
-  // row-part hops in a column-panel pass when its panel fits shared memory
-  const bool col = h->sigma_kernel != 3 && col_pass_fits(h, elem);
+  // row-part hops in the column-panel pass only on request (kind 2): the
+  // single row pass (kind 3, and the automatic choice) measured faster
+  const bool col = h->sigma_kernel == 2 && col_pass_fits(h, elem);
   int r = precision == DOCI_FP64 ? launch_row<double>(h, x, y, st, col ? 0 : 1)
                                  : launch_row<float>(h, x, y, st, col ? 0 : 1);
   if (r || !col) return r;

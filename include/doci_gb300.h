@@ -140,11 +140,11 @@ const double *doci_ham_diagonal_device(const doci_ham *ham);
  * stream (NULL = the default stream). */
 int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *stream);
 
-/* Sigma kernel selection for a handle: 0 automatic (default), 1 the
- * per-determinant gather kernel, 2 the row-tiled kernels (row pass plus the
- * column-panel pass for row-part hops), 3 the row pass alone doing all hops.
- * 2 and 3 fall back to 1 when the handle has no row tiling.  For tests and
- * tuning. */
+/* Sigma kernel selection for a handle: 0 automatic (default: the row pass
+ * when the handle has a row tiling, else the gather kernel), 1 the
+ * per-determinant gather kernel, 2 the row pass plus a column-panel pass for
+ * the row-part hops, 3 the row pass alone doing all hops.  2 and 3 fall back
+ * to 1 when the handle has no row tiling.  For tests and tuning. */
 int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
 
 /* Same on host buffers; copies in and out inside the call, synchronous. */
