@@ -89,6 +89,7 @@ def lib() -> C.CDLL:
         "doci_solve_opts_default": (None, [C.POINTER(SolveOpts)]),
         "doci_solve": (i, [vp, C.POINTER(SolveOpts), pd, C.POINTER(SolveResult)]),
         "doci_solve_footprint": (i64, [i, i, C.POINTER(SolveOpts), i]),
+        "doci_solve_trace": (i, [vp, C.POINTER(SolveOpts), pd, C.POINTER(SolveResult), pd, i, C.POINTER(i)]),
         # reference-compatible drop-in
         "fill_doci_data": (None, [C.c_char_p, C.POINTER(vp)]),
         "doci_get_diagonal": (pd, [vp]),
@@ -220,6 +221,21 @@ class Hamiltonian:
         r = SolveResult()
         _check(lib().doci_solve(self._h, C.byref(o), _dptr(v), C.byref(r)), "doci_solve")
         return r.as_dict(), v
+
+
+    def solve_trace(self, vec=None, max_records: int = 4096, **opts):
+        """doci_solve with per-iteration records: returns (result, vector,
+        trace array of rows (phase, residual, energy, seconds))."""
+        o = default_opts(**opts)
+        v = np.empty(self.D, dtype=np.float64) if vec is None else np.ascontiguousarray(vec, dtype=np.float64).copy()
+        if vec is not None and "hf_init" not in opts:
+            o.hf_init = -1
+        r = SolveResult()
+        tr = np.zeros((max_records, 4))
+        n = C.c_int()
+        _check(lib().doci_solve_trace(self._h, C.byref(o), _dptr(v), C.byref(r), _dptr(tr), max_records,
+                                      C.byref(n)), "doci_solve_trace")
+        return r.as_dict(), v, tr[:n.value].copy()
 
 
 def footprint(L: int, n_pairs: int, nroots: int = 1, **opts) -> int:

@@ -256,7 +256,16 @@ int64_t doci_solve_footprint(int L, int n_pairs, const doci_solve_opts *o, int n
 }
 
 int doci_solve(doci_ham *h, const doci_solve_opts *opts, double *vec, doci_solve_result *res) {
+  return doci_solve_trace(h, opts, vec, res, nullptr, 0, nullptr);
+}
+
+int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci_solve_result *res, double *trace,
+                     int trace_len, int *trace_count) {
   if (!h || !res) return DOCI_ERR_INVALID;
+  int count_local = 0;
+  if (!trace_count) trace_count = &count_local;
+  *trace_count = 0;
+  const double trace_t0 = now_s();
   doci_solve_opts o;
   if (opts) o = *opts; else doci_solve_opts_default(&o);
   std::memset(res, 0, sizeof *res);
@@ -285,6 +294,11 @@ int doci_solve(doci_ham *h, const doci_solve_opts *opts, double *vec, doci_solve
     a.tol = o.tol;
     a.print_table = o.print_level >= 2;
     a.print_summary = o.print_level == 1;
+    a.trace = trace;
+    a.trace_len = trace_len;
+    a.trace_t0 = trace_t0;
+    a.trace_count = trace_count;
+    a.trace_phase = 1;
     DavidsonOut out;
     int its_left = o.max_its;
     if (o.mode == DOCI_MODE_MIXED) {
@@ -295,6 +309,7 @@ int doci_solve(doci_ham *h, const doci_solve_opts *opts, double *vec, doci_solve
       a32.tol = o.mixed_tol > o.tol ? o.mixed_tol : o.tol;
       a32.stall_window = 3;
       a32.print_summary = 0;
+      a32.trace_phase = 0;
       if ((s = davidson_run<float>(op, D, h->d_diag, static_cast<float *>(t32.p), a32, st, &out, d_x))) return s;
       res->iterations_fp32 = out.iterations;
       res->energy_fp32 = out.energy;

@@ -48,11 +48,11 @@ struct DevMem {
     if (_s != DOCI_OK) return _s; \
   } while (0)
 
+}  // namespace
+
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
-
-}  // namespace
 
 int MatvecOp::apply(const void *d_x, void *d_y, int precision, cudaStream_t st) {
   if (ham) {
@@ -175,9 +175,12 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
     d_energy = energy - theta;
     energy = theta;
     if (a.print_table) std::printf("%d\t%d\t%e\t%f\n", its, 0, res, theta);
-    if (a.trace && its <= a.trace_len) {
-      a.trace[2 * (its - 1)] = res;
-      a.trace[2 * (its - 1) + 1] = theta;
+    if (a.trace && a.trace_count && *a.trace_count < a.trace_len) {
+      double *r = a.trace + 4 * (*a.trace_count)++;
+      r[0] = a.trace_phase;
+      r[1] = res;
+      r[2] = theta;
+      r[3] = now_s() - a.trace_t0;
     }
     // FP32 phase of the mixed mode: stop once the residual no longer falls
     if (a.stall_window > 0) {

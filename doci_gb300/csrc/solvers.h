@@ -32,8 +32,13 @@ struct DavidsonArgs {
   int print_table = 0;    // the -DDAVIDIT table of davidson.c:47-112
   int print_summary = 0;  // "** DAVIDSON ITERATIONS" (davidson.c:114)
   int stall_window = 0;   // > 0: stop when the residual stops halving (FP32 phase)
-  double *trace = nullptr;  // optional per-iteration (residual, energy)
+  // optional per-iteration records {phase, residual, energy, seconds since
+  // trace_t0} (4 doubles each), trace_len records at most
+  double *trace = nullptr;
   int trace_len = 0;
+  double trace_t0 = 0;
+  double trace_phase = 0;
+  int *trace_count = nullptr;  // records written so far (shared across phases)
 };
 
 struct DavidsonOut {
@@ -53,6 +58,8 @@ struct CgOut {
   double energy = 0, normq = 0, normq_g = 0, seconds = 0;
   int iterations = 0, converged = 0, return_code = 0;
 };
+
+double now_s();  // steady clock, seconds
 
 template <typename S>
 int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const DavidsonArgs &a, cudaStream_t st,

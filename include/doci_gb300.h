@@ -226,6 +226,13 @@ void doci_solve_opts_default(doci_solve_opts *opts);
 int doci_solve(doci_ham *ham, const doci_solve_opts *opts, double *vec,
                doci_solve_result *result);
 
+/* doci_solve that also records one entry per Davidson iteration into trace
+ * (4 doubles each: phase 0 = FP32, 1 = FP64; residual norm; energy; seconds
+ * since the call started), at most trace_len entries; *trace_count receives
+ * the number written.  Used to time convergence. */
+int doci_solve_trace(doci_ham *ham, const doci_solve_opts *opts, double *vec, doci_solve_result *result,
+                     double *trace, int trace_len, int *trace_count);
+
 /* Bytes of device memory a solve of ham with opts needs (admission). */
 int64_t doci_solve_footprint(int L, int n_pairs, const doci_solve_opts *opts, int nroots);
 

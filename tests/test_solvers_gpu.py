@@ -124,3 +124,16 @@ def test_foreign_matvec_through_sparse_eigensolve(fcidump, golden, dg):
     assert info == 0
     assert abs(e.value - golden["cases"][name]["davidson"]["energy"]) < 1e-8
     assert len(calls) == len(golden["cases"][name]["D_exe"]["trace"])
+
+
+def test_solve_trace_records_both_phases(synth, dg):
+    p = synth(18, 9, 43)
+    with dg.Hamiltonian.from_fcidump(p) as h:
+        r, _, tr = h.solve_trace(solver="D", tol=1e-8, max_its=300, mode="mixed", mixed_tol=1e-4)
+        r64, _, tr64 = h.solve_trace(solver="D", tol=1e-8, max_its=300)
+    assert len(tr) == r["iterations"] and len(tr64) == r64["iterations"]
+    assert (tr[: r["iterations_fp32"], 0] == 0).all() and (tr[r["iterations_fp32"]:, 0] == 1).all()
+    assert (tr64[:, 0] == 1).all()
+    assert np.all(np.diff(tr[:, 3]) >= 0) and np.all(np.diff(tr64[:, 3]) >= 0)
+    assert abs(tr[-1, 2] - r["energy"]) < 1e-12 and abs(tr64[-1, 2] - r64["energy"]) < 1e-12
+    assert abs(r["energy"] - r64["energy"]) < 1e-8
