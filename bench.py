@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge measurement")
     ap.add_argument("--max-vec", type=int, default=16, help="DAVIDSON_MAX_VEC of the convergence runs")
-    ap.add_argument("--mixed-tol", type=float, default=3e-5)
+    ap.add_argument("--mixed-tol", type=float, default=1e-5)
     return ap.parse_args()
 
 

@@ -227,7 +227,7 @@ void doci_solve_opts_default(doci_solve_opts *o) {
   o->davidson_max_vec = 30; // options.h:4
   o->hf_init = 1;
   o->mode = DOCI_MODE_FP64;
-  o->mixed_tol = 1e-4;
+  o->mixed_tol = 1e-5;
   o->print_level = 0;
   o->seed = 1;
 }
@@ -307,7 +307,7 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
       if ((s = vec_convert<double, float>(d_x, static_cast<float *>(t32.p), D, st))) return s;
       DavidsonArgs a32 = a;
       a32.tol = o.mixed_tol > o.tol ? o.mixed_tol : o.tol;
-      a32.stall_window = 3;
+      a32.stall_window = 15;
       a32.print_summary = 0;
       a32.trace_phase = 0;
       if ((s = davidson_run<float>(op, D, h->d_diag, static_cast<float *>(t32.p), a32, st, &out, d_x))) return s;

@@ -182,9 +182,11 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
       r[2] = theta;
       r[3] = now_s() - a.trace_t0;
     }
-    // FP32 phase of the mixed mode: stop once the residual no longer falls
+    // FP32 phase of the mixed mode: stop once the residual has not reached a
+    // new minimum for stall_window iterations (the FP32 noise floor; restarted
+    // Davidson residuals are not monotone, so a short window would stop early)
     if (a.stall_window > 0) {
-      if (res < 0.5 * best) {
+      if (res < best) {
         best = res;
         stall = 0;
       } else if (++stall >= a.stall_window) {
