@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--N", type=int, default=16)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
-    ap.add_argument("--kernel", choices=["auto", "gather", "row", "row1"], default="auto")
+    ap.add_argument("--kernel", choices=["auto", "gather", "row", "row1", "rowx", "rowxc"], default="auto")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -24,6 +24,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 
 namespace doci {
 namespace dev {
@@ -195,6 +196,52 @@ DOCI_HD void row_column_hops(uint32_t c, uint32_t n, int sp, int j, const uint32
     }
   }
   for (int t = 0; t < n_aa; ++t) f.across(t, c);
+}
+
+// Cross-hop index tables of the phase-ordered row pass, for a column part of
+// sp <= 16 orbitals.  For every column count j and column c (column-part set
+// M_B with colex n_j - 1 - c), 16 entries each (stride 16):
+//   rem[off[j] + 16 c + e] = (c' << 8) | m_e  for the e-th element m_e of M_B:
+//                            column c' of M_B \ m_e among the C(sp, j-1) sets;
+//   ins[off[j] + 16 c + h] = (c' << 8) | q_h  for the h-th hole q_h of M_B:
+//                            column c' of M_B u q_h among the C(sp, j+1) sets.
+// Host code (built once per handle); off has sp + 2 entries.
+inline void build_cross_tables(int sp, const uint32_t *B, int BCstride, std::vector<uint32_t> &rem,
+                               std::vector<uint32_t> &ins, std::vector<uint32_t> &off) {
+  off.assign(sp + 2, 0);
+  for (int j = 0; j <= sp; ++j) off[j + 1] = off[j] + 16u * B[sp * BCstride + j];
+  rem.assign(off[sp + 1], 0xffffffffu);
+  ins.assign(off[sp + 1], 0xffffffffu);
+  auto colex = [&](uint32_t M) {
+    uint32_t s = 0;
+    int t = 0;
+    for (int d = 0; d < sp; ++d)
+      if (M >> d & 1u) s += B[d * BCstride + (++t)];
+    return s;
+  };
+  for (int j = 0; j <= sp; ++j) {
+    const uint32_t n = B[sp * BCstride + j];
+    const uint32_t n_dn = j > 0 ? B[sp * BCstride + j - 1] : 0, n_up = j < sp ? B[sp * BCstride + j + 1] : 0;
+    for (uint32_t c = 0; c < n; ++c) {
+      // colex unrank of n - 1 - c
+      uint32_t R = n - 1 - c, M = 0;
+      int d = sp - 1;
+      for (int i = j; i >= 1; --i) {
+        while (B[d * BCstride + i] > R) --d;
+        R -= B[d * BCstride + i];
+        M |= 1u << d;
+        --d;
+      }
+      int e = 0, h = 0;
+      for (int o = 0; o < sp; ++o) {
+        if (M >> o & 1u) {
+          rem[off[j] + 16 * c + e++] = ((n_dn - 1 - colex(M & ~(1u << o))) << 8) | static_cast<uint32_t>(o);
+        } else {
+          ins[off[j] + 16 * c + h++] = ((n_up - 1 - colex(M | (1u << o))) << 8) | static_cast<uint32_t>(o);
+        }
+      }
+    }
+  }
 }
 
 }  // namespace dev

@@ -169,7 +169,7 @@ int doci_sigma(doci_ham *h, const void *d_x, void *d_y, int precision, void *str
 }
 
 int doci_ham_set_sigma_kernel(doci_ham *h, int kind) {
-  if (!h || kind < 0 || kind > 3) return DOCI_ERR_INVALID;
+  if (!h || kind < 0 || kind > 5) return DOCI_ERR_INVALID;
   h->sigma_kernel = kind;
   return DOCI_OK;
 }

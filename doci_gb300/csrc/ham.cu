@@ -12,6 +12,7 @@
 #include <cstring>
 #include <utility>
 
+#include "addressing.cuh"
 #include "internal.h"
 
 namespace doci {
@@ -54,6 +55,10 @@ void ham_release(doci_ham *h) {
   cudaFree(h->d_rowstart);
   cudaFree(h->d_sector_rs);
   cudaFree(h->d_sector_off);
+  cudaFree(h->d_rem);
+  cudaFree(h->d_ins);
+  cudaFree(h->d_tab_off);
+  h->d_rem = h->d_ins = h->d_tab_off = nullptr;
   cudaFree(h->d_panels[0]);
   cudaFree(h->d_panels[1]);
   h->d_panels[0] = h->d_panels[1] = nullptr;
@@ -228,6 +233,17 @@ int ham_build_rows(doci_ham *h) {
   DOCI_CUDA(cudaMemcpyAsync(h->d_rows, rows.data(), rows.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_rowstart, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                             h->stream));
+  {
+    std::vector<uint32_t> B(kBinomRows * kBinomCols), rem, ins, toff;
+    fill_binom_table(B.data());
+    dev::build_cross_tables(split, B.data(), kBinomCols, rem, ins, toff);
+    DOCI_CUDA(cudaMalloc(&h->d_rem, rem.size() * sizeof(uint32_t)));
+    DOCI_CUDA(cudaMalloc(&h->d_ins, ins.size() * sizeof(uint32_t)));
+    DOCI_CUDA(cudaMalloc(&h->d_tab_off, toff.size() * sizeof(uint32_t)));
+    DOCI_CUDA(cudaMemcpy(h->d_rem, rem.data(), rem.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    DOCI_CUDA(cudaMemcpy(h->d_ins, ins.data(), ins.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    DOCI_CUDA(cudaMemcpy(h->d_tab_off, toff.data(), toff.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  }
   DOCI_CUDA(cudaMalloc(&h->d_sector_off, sizeof(h->sector_off)));
   DOCI_CUDA(cudaMemcpyAsync(h->d_sector_off, h->sector_off, sizeof(h->sector_off), cudaMemcpyHostToDevice, h->stream));
   for (int v = 0; v < 2; ++v) {  // column panels of 2 (FP64) or 4 (FP32) columns

@@ -92,6 +92,9 @@ struct doci_ham {
   int *d_sector_off = nullptr;     // sector_off on the device
   int2 *d_panels[2] = {};          // column panels {k, c0}: [0] FP64 (2 columns), [1] FP32 (4 columns)
   int npanels[2] = {};
+  // cross-hop index tables of the phase-ordered row pass (addressing.cuh,
+  // build_cross_tables)
+  uint32_t *d_rem = nullptr, *d_ins = nullptr, *d_tab_off = nullptr;
 
   // host diagonal for doci_get_diagonal (lazy)
   double *h_diag = nullptr;

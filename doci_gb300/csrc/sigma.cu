@@ -320,6 +320,207 @@ bool row_kernel_fits(const doci_ham *h, size_t elem) {
 }
 
 // ---------------------------------------------------------------------------
+// Phase-ordered row pass.  Same row tiling as sigma_row_kernel, but the
+// cross hops are taken one source row at a time: each of the rows R u q
+// (column part -> row part) and R \ m (row part -> column part) is staged in
+// shared memory with cp.async, and every column of the output row gathers
+// its neighbours from it, with the neighbour columns read from the
+// precomputed tables (build_cross_tables).  The output row accumulates in
+// shared memory across phases.  Phase 0 does the diagonal, the column-part
+// hops (own row staged) and, when asked, the row-part hops (aligned loads).
+// ---------------------------------------------------------------------------
+constexpr int kRowxThreads = 256;
+
+template <typename Real>
+struct RowxTables {
+  uint32_t binom[17 * kBinomCols];  // binomials C(n, k), n <= 16 (the column part)
+  Real Kb[16 * 16];                 // K between column-part orbitals
+  Real Kx[16];                      // K row of the current cross phase
+  uint32_t aa_rs[kMaxIntraRow];
+  Real aa_K[kMaxIntraRow];
+  uint32_t ab_rs[kMaxRowPart];
+  int ab_m[kMaxRowPart];
+  uint32_t ba_rs[kMaxRowPart];
+  int ba_q[kMaxRowPart];
+  int n_aa, n_ab, n_ba;
+};
+
+template <int Bytes>
+__device__ __forceinline__ void cp_async(void *smem, const void *g) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(g), "n"(Bytes));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <typename Real>
+__device__ __forceinline__ void stage_row(Real *buf, const Real *src, uint32_t n) {
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) cp_async<sizeof(Real)>(buf + i, src + i);
+  cp_async_wait_all();
+}
+
+// acc[c] += sum over the first `cnt` table entries (neighbour column << 8 | orbital)
+template <typename Real>
+__device__ __forceinline__ Real table_gather(const uint32_t *__restrict__ ent, int cnt, const Real *Kx, const Real *buf) {
+  Real a = 0;
+  const uint4 *e4 = reinterpret_cast<const uint4 *>(ent);
+#pragma unroll
+  for (int i4 = 0; i4 < 4; ++i4) {
+    if (4 * i4 < cnt) {
+      const uint4 v = __ldg(e4 + i4);
+      a += Kx[v.x & 255u] * buf[v.x >> 8];
+      if (4 * i4 + 1 < cnt) a += Kx[v.y & 255u] * buf[v.y >> 8];
+      if (4 * i4 + 2 < cnt) a += Kx[v.z & 255u] * buf[v.z >> 8];
+      if (4 * i4 + 3 < cnt) a += Kx[v.w & 255u] * buf[v.w >> 8];
+    }
+  }
+  return a;
+}
+
+template <typename Real, int NHB>
+__global__ void __launch_bounds__(kRowxThreads, 2)
+sigma_rowx_kernel(RowShape s, int with_across, uint32_t row_pad, const uint2 *__restrict__ rows,
+                  const uint32_t *__restrict__ rowstart_of, const uint32_t *__restrict__ g_binom,
+                  const Real *__restrict__ g_K, const uint32_t *__restrict__ rem_tab,
+                  const uint32_t *__restrict__ ins_tab, const uint32_t *__restrict__ tab_off,
+                  const Real *__restrict__ diag, const Real *__restrict__ x, Real *__restrict__ y) {
+  __shared__ RowxTables<Real> tb;
+  extern __shared__ __align__(16) unsigned char rowx_smem[];
+  Real *acc = reinterpret_cast<Real *>(rowx_smem);
+  Real *buf = acc + row_pad;
+  const int sp = s.split, na = s.na;
+  for (int t = threadIdx.x; t < 17 * kBinomCols; t += blockDim.x) tb.binom[t] = g_binom[t];
+  for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+    const int m = t >> 4, q = t & 15;
+    tb.Kb[t] = (m < sp && q < sp) ? g_K[m * 32 + q] : Real(0);
+  }
+  const uint32_t *B = tb.binom;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  for (int row = blockIdx.x; row < s.nrows; row += gridDim.x) {
+    const uint2 rw = rows[row];
+    const uint32_t rstart = rw.x, mask = rw.y & 0xffffffu;
+    const int k = static_cast<int>(rw.y >> 24), j = s.N - k;
+    __syncthreads();
+    if (warp == 0) {
+      const bool live = lane < na;
+      const bool in_r = live && ((mask >> lane) & 1u);
+      const bool hole = live && !in_r;
+      const uint32_t eb = __ballot_sync(0xffffffffu, in_r), hb = __ballot_sync(0xffffffffu, hole);
+      const uint32_t below = (1u << lane) - 1u;
+      if (in_r) {
+        const int e = __popc(eb & below);
+        tb.ab_rs[e] = rowstart_of[mask & ~(1u << lane)];
+        tb.ab_m[e] = sp + lane;
+      }
+      if (hole) {
+        const int h = __popc(hb & below);
+        tb.ba_rs[h] = rowstart_of[mask | (1u << lane)];
+        tb.ba_q[h] = sp + lane;
+      }
+      const int ne = __popc(eb), nhl = __popc(hb);
+      if (lane == 0) {
+        tb.n_ab = j < sp ? ne : 0;
+        tb.n_ba = j > 0 ? nhl : 0;
+        tb.n_aa = with_across ? ne * nhl : 0;
+      }
+      for (int t = lane; with_across && t < ne * nhl; t += 32) {
+        const int e = t / nhl, h = t % nhl;
+        const int a_e = __fns(eb, 0, e + 1), a_h = __fns(hb, 0, h + 1);
+        tb.aa_rs[t] = rowstart_of[(mask & ~(1u << a_e)) | (1u << a_h)];
+        tb.aa_K[t] = g_K[(sp + a_e) * 32 + sp + a_h];
+      }
+    }
+    const uint32_t n = B[sp * kBinomCols + j];
+    stage_row(buf, x + rstart, n);
+    __syncthreads();
+    // phase 0: diagonal, column-part hops from the staged own row, row-part hops
+    const int n_aa = tb.n_aa, n_ab = tb.n_ab, n_ba = tb.n_ba;
+    for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) {
+      const uint32_t p = n - 1 - c;
+      const uint32_t Mb = dev::colex_unrank<kBinomCols>(p, sp, j, B);
+      dev::Neighbours<NHB, kBinomCols> nb;
+      nb.precompute(Mb, p, sp, sp - j, B);
+      struct In {
+        const Real *Kb, *buf;
+        const Real *Krow;
+        Real a;
+        __device__ __forceinline__ void begin(int m) { Krow = Kb + m * 16; }
+        __device__ __forceinline__ void hop(int, int q, uint32_t cc) { a += Krow[q] * buf[cc]; }
+      } f{tb.Kb, buf, tb.Kb, diag[rstart + c] * buf[c]};
+      nb.visit(Mb, p, n - 1, j, sp - j, B, f);
+      Real a2 = 0;
+      int t = 0;
+      for (; t + 4 <= n_aa; t += 4) {
+        const Real v0 = __ldg(x + tb.aa_rs[t] + c), v1 = __ldg(x + tb.aa_rs[t + 1] + c);
+        const Real v2 = __ldg(x + tb.aa_rs[t + 2] + c), v3 = __ldg(x + tb.aa_rs[t + 3] + c);
+        a2 += tb.aa_K[t] * v0 + tb.aa_K[t + 1] * v1 + tb.aa_K[t + 2] * v2 + tb.aa_K[t + 3] * v3;
+      }
+      for (; t < n_aa; ++t) a2 += tb.aa_K[t] * __ldg(x + tb.aa_rs[t] + c);
+      acc[c] = f.a + a2;
+    }
+    // column part -> row part: sources R u q, one at a time
+    if (n_ba > 0) {
+      const uint32_t n_dn = B[sp * kBinomCols + j - 1];
+      const uint32_t *remj = rem_tab + tab_off[j];
+      for (int t = 0; t < n_ba; ++t) {
+        __syncthreads();
+        if (threadIdx.x < 16) tb.Kx[threadIdx.x] = threadIdx.x < sp ? g_K[threadIdx.x * 32 + tb.ba_q[t]] : Real(0);
+        stage_row(buf, x + tb.ba_rs[t], n_dn);
+        __syncthreads();
+        for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) acc[c] += table_gather(remj + 16 * c, j, tb.Kx, buf);
+      }
+    }
+    // row part -> column part: sources R \ m, one at a time
+    if (n_ab > 0) {
+      const uint32_t n_up = B[sp * kBinomCols + j + 1];
+      const uint32_t *insj = ins_tab + tab_off[j];
+      for (int t = 0; t < n_ab; ++t) {
+        __syncthreads();
+        if (threadIdx.x < 16) tb.Kx[threadIdx.x] = threadIdx.x < sp ? g_K[tb.ab_m[t] * 32 + threadIdx.x] : Real(0);
+        stage_row(buf, x + tb.ab_rs[t], n_up);
+        __syncthreads();
+        for (uint32_t c = threadIdx.x; c < n; c += blockDim.x)
+          acc[c] += table_gather(insj + 16 * c, sp - j, tb.Kx, buf);
+      }
+    }
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) y[rstart + c] = acc[c];
+  }
+}
+
+template <typename Real>
+int launch_rowx(const doci_ham *h, const void *x, void *y, cudaStream_t st, int with_across) {
+  const RowShape s{h->D, h->L, h->N, h->split, h->L - h->split, h->nrows};
+  const uint32_t pad = (static_cast<uint32_t>(h->max_row) + 3u) & ~3u;
+  const size_t dyn = 2 * static_cast<size_t>(pad) * sizeof(Real);
+  auto kern = sigma_rowx_kernel<Real, 16>;
+  static size_t configured = 0;
+  static int blocks_per_sm = 1;
+  if (configured != dyn) {
+    DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kRowxThreads, dyn);
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    configured = dyn;
+  }
+  int grid = device_sm_count() * blocks_per_sm;
+  if (grid > h->nrows) grid = h->nrows;
+  const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
+                                                   : reinterpret_cast<const Real *>(h->d_Kmir32);
+  const Real *dg = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_diag)
+                                                    : reinterpret_cast<const Real *>(h->d_diag32);
+  kern<<<grid, kRowxThreads, dyn, st>>>(s, with_across, pad, reinterpret_cast<const uint2 *>(h->d_rows),
+                                        h->d_rowstart, h->d_binom, K, h->d_rem, h->d_ins, h->d_tab_off, dg,
+                                        static_cast<const Real *>(x), static_cast<Real *>(y));
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+bool rowx_fits(const doci_ham *h, size_t elem) {
+  if (!h->d_rem || h->split > 16) return false;
+  return 2 * (static_cast<size_t>(h->max_row) + 3) * elem <= 210 * 1024;
+}
+
+// ---------------------------------------------------------------------------
 // Column-panel pass: the row-part hops (both orbitals in the row part) keep
 // the column and change the row, within one sector (rows with the same
 // number k of row-part elements).  One block loads W consecutive columns of
@@ -370,8 +571,10 @@ sigma_col_kernel(ColShape s, const int2 *__restrict__ panels, int npanels, const
     const uint32_t *rs = sector_rs + sector_off[k];
     for (uint32_t t = threadIdx.x; t < nr * W; t += blockDim.x) {
       const uint32_t r = t / W, w = t % W;
-      P[t] = w < wc ? x[rs[r] + c0 + w] : Real(0);
+      if (w < wc) cp_async<sizeof(Real)>(P + t, x + rs[r] + c0 + w);
+      else P[t] = Real(0);
     }
+    cp_async_wait_all();
     __syncthreads();
     const Real *Kbase = K + sp * 32 + sp;
     for (uint32_t r = threadIdx.x; r < nr; r += blockDim.x) {
@@ -454,6 +657,14 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
   bool row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
   if (!row) return precision == DOCI_FP64 ? launch_typed<double>(h, x, y, st) : launch_typed<float>(h, x, y, st);
+  if ((h->sigma_kernel == 0 || h->sigma_kernel >= 4) && rowx_fits(h, elem)) {
+    // phase-ordered row pass; kind 5 moves the row-part hops to the column pass
+    const bool colp = h->sigma_kernel == 5 && col_pass_fits(h, elem);
+    int r = precision == DOCI_FP64 ? launch_rowx<double>(h, x, y, st, colp ? 0 : 1)
+                                   : launch_rowx<float>(h, x, y, st, colp ? 0 : 1);
+    if (r || !colp) return r;
+    return precision == DOCI_FP64 ? launch_col<double>(h, x, y, st) : launch_col<float>(h, x, y, st);
+  }
   // row-part hops in the column-panel pass only on request (kind 2): the
   // single row pass (kind 3, and the automatic choice) measured faster
   const bool col = h->sigma_kernel == 2 && col_pass_fits(h, elem);

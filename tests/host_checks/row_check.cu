@@ -82,6 +82,8 @@ int main(int argc, char **argv) {
     for (int b = 0; b < BC; ++b) x.B[a * BC + b] = static_cast<uint32_t>(binom(a, b));
   const int na = x.L - x.sp;
   long bad = 0, dets = 0, rows = 0;
+  std::vector<uint32_t> rem_tab, ins_tab, tab_off;
+  doci::dev::build_cross_tables(x.sp, x.B.data(), BC, rem_tab, ins_tab, tab_off);
   uint64_t covered = 0;
   for (uint32_t R = 0; R < (1u << na); ++R) {
     if (!row_valid(x, R)) continue;
@@ -129,6 +131,29 @@ int main(int argc, char **argv) {
                                          static_cast<int>(aa_rs.size()), f);
       if (f.hops != static_cast<long>(x.N) * (x.L - x.N)) ++bad;
       bad += f.bad;
+      // the phase-ordered pass: cross hops through the tables
+      {
+        long th = 0;
+        auto chk = [&](uint64_t rank, uint32_t nb_set) {
+          ++th;
+          if (rank != direct_rank_mirrored(nb_set, x.L, x.N)) ++bad;
+        };
+        for (int t = 0; t < n_ba; ++t)
+          for (int e = 0; e < j; ++e) {
+            const uint32_t v = rem_tab[tab_off[j] + 16 * c + e];
+            const int m = static_cast<int>(v & 255u);
+            if (!(Mb >> m & 1u) || (v >> 8) >= ba_len[t]) { ++bad; continue; }
+            chk(ba_rs[t] + (v >> 8), (T & ~(1u << m)) | (1u << ba_q[t]));
+          }
+        for (int t = 0; t < n_ab; ++t)
+          for (int h = 0; h < x.sp - j; ++h) {
+            const uint32_t v = ins_tab[tab_off[j] + 16 * c + h];
+            const int q = static_cast<int>(v & 255u);
+            if ((Mb >> q & 1u) || q >= x.sp || (v >> 8) >= ab_len[t]) { ++bad; continue; }
+            chk(ab_rs[t] + (v >> 8), (T & ~(1u << ab_m[t])) | (1u << q));
+          }
+        if (th != static_cast<long>(n_ba) * j + static_cast<long>(n_ab) * (x.sp - j)) ++bad;
+      }
       ++dets;
     }
   }
