@@ -657,7 +657,10 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
   bool row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
   if (!row) return precision == DOCI_FP64 ? launch_typed<double>(h, x, y, st) : launch_typed<float>(h, x, y, st);
-  if ((h->sigma_kernel == 0 || h->sigma_kernel >= 4) && rowx_fits(h, elem)) {
+  // automatic: the phase-ordered pass for FP64 (measured faster there), the
+  // single row pass for FP32 (measured faster there)
+  const bool want_rowx = h->sigma_kernel >= 4 || (h->sigma_kernel == 0 && precision == DOCI_FP64);
+  if (want_rowx && rowx_fits(h, elem)) {
     // phase-ordered row pass; kind 5 moves the row-part hops to the column pass
     const bool colp = h->sigma_kernel == 5 && col_pass_fits(h, elem);
     int r = precision == DOCI_FP64 ? launch_rowx<double>(h, x, y, st, colp ? 0 : 1)

@@ -140,11 +140,13 @@ const double *doci_ham_diagonal_device(const doci_ham *ham);
  * stream (NULL = the default stream). */
 int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *stream);
 
-/* Sigma kernel selection for a handle: 0 automatic (default: the row pass
- * when the handle has a row tiling, else the gather kernel), 1 the
- * per-determinant gather kernel, 2 the row pass plus a column-panel pass for
- * the row-part hops, 3 the row pass alone doing all hops.  2 and 3 fall back
- * to 1 when the handle has no row tiling.  For tests and tuning. */
+/* Sigma kernel selection for a handle: 0 automatic (default: with a row
+ * tiling, kind 3 for FP32 and kind 4 for FP64, the fastest measured; else
+ * kind 1), 1 the per-determinant gather kernel, 2 the row pass plus a
+ * column-panel pass for the row-part hops, 3 the row pass alone doing all
+ * hops, 4 the phase-ordered row pass (cross hops staged one source row at a
+ * time), 5 kind 4 plus the column-panel pass.  2-5 fall back to 1 when the
+ * handle has no row tiling.  For tests and tuning. */
 int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
 
 /* Same on host buffers; copies in and out inside the call, synchronous. */
