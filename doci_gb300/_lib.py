@@ -56,6 +56,25 @@ class SolveResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("nroots", C.c_int), ("max_vec", C.c_int), ("max_its", C.c_int), ("tol", C.c_double),
+                ("mode", C.c_int), ("mixed_tol", C.c_double), ("workers", C.c_int), ("hbm_budget", C.c_int64)]
+
+
+class RootResult(C.Structure):
+    _fields_ = [("energy", C.c_double * 8), ("residual", C.c_double * 8), ("energy_fp32", C.c_double * 8),
+                ("nroots", C.c_int), ("iterations", C.c_int), ("iterations_fp32", C.c_int), ("sigmas", C.c_int),
+                ("converged", C.c_int), ("status", C.c_int), ("queued_s", C.c_double), ("start_s", C.c_double),
+                ("end_s", C.c_double)]
+
+    def as_dict(self):
+        n = self.nroots
+        return {"energies": list(self.energy[:n]), "residuals": list(self.residual[:n]),
+                "energies_fp32": list(self.energy_fp32[:n]), "iterations": self.iterations,
+                "iterations_fp32": self.iterations_fp32, "sigmas": self.sigmas, "converged": self.converged,
+                "status": self.status, "queued_s": self.queued_s, "start_s": self.start_s, "end_s": self.end_s}
+
+
 _LIB = None
 MATVEC_FN = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
 
@@ -90,6 +109,17 @@ def lib() -> C.CDLL:
         "doci_solve": (i, [vp, C.POINTER(SolveOpts), pd, C.POINTER(SolveResult)]),
         "doci_solve_footprint": (i64, [i, i, C.POINTER(SolveOpts), i]),
         "doci_solve_trace": (i, [vp, C.POINTER(SolveOpts), pd, C.POINTER(SolveResult), pd, i, C.POINTER(i)]),
+        "doci_batch_opts_default": (None, [C.POINTER(BatchOpts)]),
+        "doci_roots_footprint": (i64, [i, i, C.POINTER(BatchOpts)]),
+        "doci_solve_roots": (i, [vp, C.POINTER(BatchOpts), C.POINTER(RootResult), pd]),
+        "doci_batch_solve": (i, [i, C.POINTER(vp), C.POINTER(BatchOpts), C.POINTER(RootResult)]),
+        "doci_server_create": (i, [C.POINTER(BatchOpts), C.POINTER(vp)]),
+        "doci_server_submit": (i, [vp, i, i, d, pd, pd, C.POINTER(i64)]),
+        "doci_server_submit_fcidump": (i, [vp, C.c_char_p, C.POINTER(i64)]),
+        "doci_server_poll": (i, [vp, i64, C.POINTER(RootResult)]),
+        "doci_server_wait": (i, [vp, i64, C.POINTER(RootResult)]),
+        "doci_server_stats": (i, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
+        "doci_server_destroy": (None, [vp]),
         # reference-compatible drop-in
         "fill_doci_data": (None, [C.c_char_p, C.POINTER(vp)]),
         "doci_get_diagonal": (pd, [vp]),
@@ -236,6 +266,81 @@ class Hamiltonian:
         _check(lib().doci_solve_trace(self._h, C.byref(o), _dptr(v), C.byref(r), _dptr(tr), max_records,
                                       C.byref(n)), "doci_solve_trace")
         return r.as_dict(), v, tr[:n.value].copy()
+
+
+def batch_opts(**kw) -> BatchOpts:
+    o = BatchOpts()
+    lib().doci_batch_opts_default(C.byref(o))
+    for k, v in kw.items():
+        if k == "mode" and isinstance(v, str):
+            v = {"fp64": MODE_FP64, "mixed": MODE_MIXED}[v]
+        setattr(o, k, v)
+    return o
+
+
+def solve_roots(ham: "Hamiltonian", vectors: bool = False, **kw):
+    o = batch_opts(**kw)
+    r = RootResult()
+    v = np.empty((o.nroots, ham.D)) if vectors else None
+    _check(lib().doci_solve_roots(ham.handle, C.byref(o), C.byref(r), _dptr(v) if vectors else None),
+           "doci_solve_roots")
+    return (r.as_dict(), v) if vectors else r.as_dict()
+
+
+def batch_solve(hams, **kw):
+    o = batch_opts(**kw)
+    arr = (C.c_void_p * len(hams))(*[h.handle.value for h in hams])
+    res = (RootResult * len(hams))()
+    st = lib().doci_batch_solve(len(hams), arr, C.byref(o), res)
+    return st, [r.as_dict() for r in res]
+
+
+class Server:
+    """The request server (doci_server_*): submit integrals, get tickets."""
+
+    def __init__(self, **kw):
+        self._o = batch_opts(**kw)
+        self._s = C.c_void_p()
+        _check(lib().doci_server_create(C.byref(self._o), C.byref(self._s)), "doci_server_create")
+
+    def submit(self, L, n_pairs, one, two, core=0.0) -> int:
+        one = np.ascontiguousarray(one, dtype=np.float64).reshape(-1)
+        two = np.ascontiguousarray(two, dtype=np.float64).reshape(-1)
+        t = C.c_int64()
+        _check(lib().doci_server_submit(self._s, L, n_pairs, core, _dptr(one), _dptr(two), C.byref(t)),
+               "doci_server_submit")
+        return t.value
+
+    def submit_fcidump(self, path) -> int:
+        t = C.c_int64()
+        _check(lib().doci_server_submit_fcidump(self._s, os.fsencode(path), C.byref(t)), "doci_server_submit_fcidump")
+        return t.value
+
+    def poll(self, ticket):
+        r = RootResult()
+        st = lib().doci_server_poll(self._s, ticket, C.byref(r))
+        return st, (r.as_dict() if st == 0 else None)
+
+    def wait(self, ticket):
+        r = RootResult()
+        _check(lib().doci_server_wait(self._s, ticket, C.byref(r)), "doci_server_wait")
+        return r.as_dict()
+
+    def stats(self):
+        v = [C.c_int64() for _ in range(4)]
+        _check(lib().doci_server_stats(self._s, *[C.byref(x) for x in v]), "doci_server_stats")
+        return dict(zip(("submitted", "finished", "running", "bytes_in_use"), [x.value for x in v]))
+
+    def close(self):
+        if self._s:
+            lib().doci_server_destroy(self._s)
+            self._s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def footprint(L: int, n_pairs: int, nroots: int = 1, **opts) -> int:

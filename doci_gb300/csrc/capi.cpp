@@ -46,9 +46,13 @@ bool reg_has(const void *h) {
 // stream, so work queued by the caller on it is ordered before ours.
 cudaStream_t pick(doci_ham *, void *stream) { return static_cast<cudaStream_t>(stream); }
 
+// stream-ordered device buffer (freeing does not synchronise the device)
 struct DevBuf {
   void *p = nullptr;
-  ~DevBuf() { cudaFree(p); }
+  cudaStream_t st = nullptr;
+  ~DevBuf() {
+    if (p) cudaFreeAsync(p, st);
+  }
 };
 
 // fatal-error convention of the reference's entry points
@@ -272,7 +276,8 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
   const size_t D = h->D;
   cudaStream_t st = h->stream;
   DevBuf x;
-  DOCI_CUDA(cudaMalloc(&x.p, sizeof(double) * D));
+  x.st = st;
+  DOCI_CUDA(cudaMallocAsync(&x.p, sizeof(double) * D, st));
   double *d_x = static_cast<double *>(x.p);
   int s;
   if (o.hf_init < 0) {
@@ -303,7 +308,8 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
     int its_left = o.max_its;
     if (o.mode == DOCI_MODE_MIXED) {
       DevBuf t32;
-      DOCI_CUDA(cudaMalloc(&t32.p, sizeof(float) * D));
+      t32.st = st;
+  DOCI_CUDA(cudaMallocAsync(&t32.p, sizeof(float) * D, st));
       if ((s = vec_convert<double, float>(d_x, static_cast<float *>(t32.p), D, st))) return s;
       DavidsonArgs a32 = a;
       a32.tol = o.mixed_tol > o.tol ? o.mixed_tol : o.tol;
@@ -318,7 +324,8 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
     }
     a.max_its = its_left;
     DevBuf t;
-    DOCI_CUDA(cudaMalloc(&t.p, sizeof(double) * D));
+    t.st = st;
+  DOCI_CUDA(cudaMallocAsync(&t.p, sizeof(double) * D, st));
     DOCI_CUDA(cudaMemcpyAsync(t.p, d_x, sizeof(double) * D, cudaMemcpyDeviceToDevice, st));
     if ((s = davidson_run<double>(op, D, h->d_diag, static_cast<double *>(t.p), a, st, &out, d_x))) return s;
     res->energy = out.energy;
@@ -487,7 +494,8 @@ struct SolverContext {
       if (h && diagonal == h->h_diag) {
         d_diag = h->d_diag;
       } else {
-        DOCI_CUDA(cudaMalloc(&diag_buf.p, sizeof(double) * n));
+        diag_buf.st = st;
+  DOCI_CUDA(cudaMallocAsync(&diag_buf.p, sizeof(double) * n, st));
         DOCI_CUDA(cudaMemcpyAsync(diag_buf.p, diagonal, sizeof(double) * n, cudaMemcpyHostToDevice, st));
         d_diag = static_cast<const double *>(diag_buf.p);
       }
@@ -512,7 +520,8 @@ int davidson(double *result, double *energy, int max_vectors, int keep_deflate, 
   if (st) die_cuda("davidson", st);
   if (!ctx.d_diag) die_cuda("davidson (no diagonal)", DOCI_ERR_INVALID);
   DevBuf t, x;
-  if (cudaMalloc(&t.p, sizeof(double) * n) || cudaMalloc(&x.p, sizeof(double) * n))
+  t.st = x.st = ctx.st;
+  if (cudaMallocAsync(&t.p, sizeof(double) * n, ctx.st) || cudaMallocAsync(&x.p, sizeof(double) * n, ctx.st))
     die_cuda("davidson", DOCI_ERR_OUT_OF_MEMORY);
   cudaMemcpyAsync(t.p, result, sizeof(double) * n, cudaMemcpyHostToDevice, ctx.st);
   DavidsonArgs a;
@@ -543,7 +552,8 @@ int ray_q(void (*matvec)(double *, double *, void *), double *M, double *vec, in
   int st = ctx.init(matvec, vdat, precond, n);
   if (st) die_cuda("ray_q", st);
   DevBuf x;
-  if (cudaMalloc(&x.p, sizeof(double) * n)) die_cuda("ray_q", DOCI_ERR_OUT_OF_MEMORY);
+  x.st = ctx.st;
+  if (cudaMallocAsync(&x.p, sizeof(double) * n, ctx.st)) die_cuda("ray_q", DOCI_ERR_OUT_OF_MEMORY);
   cudaMemcpyAsync(x.p, vec, sizeof(double) * n, cudaMemcpyHostToDevice, ctx.st);
   CgArgs a;
   a.max_its = max_its;

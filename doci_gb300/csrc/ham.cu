@@ -9,6 +9,7 @@
 
 #include <cstdlib>
 #include <algorithm>
+#include <mutex>
 #include <cstring>
 #include <utility>
 
@@ -41,47 +42,60 @@ int device_sm_count() {
   return sms;
 }
 
+// Device buffers of a handle come from the stream-ordered allocator on the
+// handle's stream: creating and destroying handles while other solves run
+// (the request server) then never synchronises the whole device.
+static void release_async(void *p, cudaStream_t st) {
+  if (p) cudaFreeAsync(p, st);
+}
+
 void ham_release(doci_ham *h) {
   if (!h) return;
-  cudaFree(h->d_binom);
-  cudaFree(h->d_Kmir64);
-  cudaFree(h->d_Kmir32);
-  cudaFree(h->d_tab64);
-  cudaFree(h->d_diag);
-  cudaFree(h->d_diag32);
-  cudaFree(h->d_stage_x);
-  cudaFree(h->d_stage_y);
-  cudaFree(h->d_rows);
-  cudaFree(h->d_rowstart);
-  cudaFree(h->d_sector_rs);
-  cudaFree(h->d_sector_off);
-  cudaFree(h->d_rem);
-  cudaFree(h->d_ins);
-  cudaFree(h->d_tab_off);
-  h->d_rem = h->d_ins = h->d_tab_off = nullptr;
-  cudaFree(h->d_panels[0]);
-  cudaFree(h->d_panels[1]);
-  h->d_panels[0] = h->d_panels[1] = nullptr;
-  h->d_sector_off = nullptr;
-  h->d_rows = h->d_rowstart = h->d_sector_rs = nullptr;
+  cudaStream_t st = h->stream;
+  void *bufs[] = {h->d_binom, h->d_Kmir64, h->d_Kmir32, h->d_tab64, h->d_diag, h->d_diag32, h->d_stage_x,
+                  h->d_stage_y, h->d_rows, h->d_rowstart, h->d_sector_rs, h->d_sector_off, h->d_panels[0],
+                  h->d_panels[1], h->d_rem, h->d_ins, h->d_tab_off};
+  for (void *p : bufs) release_async(p, st);
   if (h->h_diag) cudaFreeHost(h->h_diag);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  if (st) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
   h->d_binom = nullptr;
   h->d_Kmir64 = h->d_tab64 = h->d_diag = nullptr;
   h->d_Kmir32 = h->d_diag32 = nullptr;
   h->d_stage_x = h->d_stage_y = nullptr;
+  h->d_rows = h->d_rowstart = h->d_sector_rs = nullptr;
+  h->d_sector_off = nullptr;
+  h->d_panels[0] = h->d_panels[1] = nullptr;
+  h->d_rem = h->d_ins = h->d_tab_off = nullptr;
   h->h_diag = nullptr;
   h->stream = nullptr;
 }
 
+// keep freed memory in the device's default pool for reuse
+void keep_pool_memory() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t threshold = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    cudaGetLastError();
+  });
+}
+
 int ham_stage(doci_ham *h, size_t bytes) {
   if (h->stage_bytes >= bytes) return DOCI_OK;
-  cudaFree(h->d_stage_x);
-  cudaFree(h->d_stage_y);
+  release_async(h->d_stage_x, h->stream);
+  release_async(h->d_stage_y, h->stream);
   h->d_stage_x = h->d_stage_y = nullptr;
   h->stage_bytes = 0;
-  DOCI_CUDA(cudaMalloc(&h->d_stage_x, bytes));
-  DOCI_CUDA(cudaMalloc(&h->d_stage_y, bytes));
+  DOCI_CUDA(cudaMallocAsync(&h->d_stage_x, bytes, h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_stage_y, bytes, h->stream));
   h->stage_bytes = bytes;
   return DOCI_OK;
 }
@@ -120,6 +134,7 @@ int ham_build(doci_ham *h, const Integrals &in) {
     }
   }
   cudaGetDevice(&h->device);
+  keep_pool_memory();
   DOCI_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
 
   std::vector<uint32_t> binom(kBinomRows * kBinomCols);
@@ -136,12 +151,12 @@ int ham_build(doci_ham *h, const Integrals &in) {
   std::memcpy(tab.data() + n, h->J2.data(), n2 * sizeof(double));
   std::memcpy(tab.data() + n + n2, h->Kx.data(), n2 * sizeof(double));
 
-  DOCI_CUDA(cudaMalloc(&h->d_binom, binom.size() * sizeof(uint32_t)));
-  DOCI_CUDA(cudaMalloc(&h->d_Kmir64, 32 * 32 * sizeof(double)));
-  DOCI_CUDA(cudaMalloc(&h->d_Kmir32, 32 * 32 * sizeof(float)));
-  DOCI_CUDA(cudaMalloc(&h->d_tab64, tab.size() * sizeof(double)));
-  DOCI_CUDA(cudaMalloc(&h->d_diag, static_cast<size_t>(h->D) * sizeof(double)));
-  DOCI_CUDA(cudaMalloc(&h->d_diag32, static_cast<size_t>(h->D) * sizeof(float)));
+  DOCI_CUDA(cudaMallocAsync(&h->d_binom, binom.size() * sizeof(uint32_t), h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_Kmir64, 32 * 32 * sizeof(double), h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_Kmir32, 32 * 32 * sizeof(float), h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_tab64, tab.size() * sizeof(double), h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_diag, static_cast<size_t>(h->D) * sizeof(double), h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_diag32, static_cast<size_t>(h->D) * sizeof(float), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_binom, binom.data(), binom.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_Kmir64, kmir.data(), kmir.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_Kmir32, kmir32.data(), kmir32.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
@@ -228,8 +243,8 @@ int ham_build_rows(doci_ham *h) {
     sector[h->sector_off[k] + (binom64(na, k) - 1 - colex)] = start[mask];
   }
   h->max_sector_rows = max_sector;
-  DOCI_CUDA(cudaMalloc(&h->d_rows, rows.size() * sizeof(uint32_t)));
-  DOCI_CUDA(cudaMalloc(&h->d_rowstart, start.size() * sizeof(uint32_t)));
+  DOCI_CUDA(cudaMallocAsync(&h->d_rows, rows.size() * sizeof(uint32_t), h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_rowstart, start.size() * sizeof(uint32_t), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_rows, rows.data(), rows.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_rowstart, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                             h->stream));
@@ -237,14 +252,16 @@ int ham_build_rows(doci_ham *h) {
     std::vector<uint32_t> B(kBinomRows * kBinomCols), rem, ins, toff;
     fill_binom_table(B.data());
     dev::build_cross_tables(split, B.data(), kBinomCols, rem, ins, toff);
-    DOCI_CUDA(cudaMalloc(&h->d_rem, rem.size() * sizeof(uint32_t)));
-    DOCI_CUDA(cudaMalloc(&h->d_ins, ins.size() * sizeof(uint32_t)));
-    DOCI_CUDA(cudaMalloc(&h->d_tab_off, toff.size() * sizeof(uint32_t)));
-    DOCI_CUDA(cudaMemcpy(h->d_rem, rem.data(), rem.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    DOCI_CUDA(cudaMemcpy(h->d_ins, ins.data(), ins.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    DOCI_CUDA(cudaMemcpy(h->d_tab_off, toff.data(), toff.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    DOCI_CUDA(cudaMallocAsync(&h->d_rem, rem.size() * sizeof(uint32_t), h->stream));
+    DOCI_CUDA(cudaMallocAsync(&h->d_ins, ins.size() * sizeof(uint32_t), h->stream));
+    DOCI_CUDA(cudaMallocAsync(&h->d_tab_off, toff.size() * sizeof(uint32_t), h->stream));
+    DOCI_CUDA(cudaMemcpyAsync(h->d_rem, rem.data(), rem.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    DOCI_CUDA(cudaMemcpyAsync(h->d_ins, ins.data(), ins.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    DOCI_CUDA(cudaMemcpyAsync(h->d_tab_off, toff.data(), toff.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                              h->stream));
+    DOCI_CUDA(cudaStreamSynchronize(h->stream));
   }
-  DOCI_CUDA(cudaMalloc(&h->d_sector_off, sizeof(h->sector_off)));
+  DOCI_CUDA(cudaMallocAsync(&h->d_sector_off, sizeof(h->sector_off), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_sector_off, h->sector_off, sizeof(h->sector_off), cudaMemcpyHostToDevice, h->stream));
   for (int v = 0; v < 2; ++v) {  // column panels of 2 (FP64) or 4 (FP32) columns
     const int W = v == 0 ? 2 : 4;
@@ -256,11 +273,11 @@ int ham_build_rows(doci_ham *h) {
       for (uint64_t c0 = 0; c0 < ncol; c0 += W) pv.push_back(make_int2(k, static_cast<int>(c0)));
     }
     h->npanels[v] = static_cast<int>(pv.size());
-    DOCI_CUDA(cudaMalloc(&h->d_panels[v], pv.size() * sizeof(int2)));
+    DOCI_CUDA(cudaMallocAsync(&h->d_panels[v], pv.size() * sizeof(int2), h->stream));
     DOCI_CUDA(cudaMemcpyAsync(h->d_panels[v], pv.data(), pv.size() * sizeof(int2), cudaMemcpyHostToDevice, h->stream));
     DOCI_CUDA(cudaStreamSynchronize(h->stream));
   }
-  DOCI_CUDA(cudaMalloc(&h->d_sector_rs, sector.size() * sizeof(uint32_t)));
+  DOCI_CUDA(cudaMallocAsync(&h->d_sector_rs, sector.size() * sizeof(uint32_t), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_sector_rs, sector.data(), sector.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                             h->stream));
   DOCI_CUDA(cudaStreamSynchronize(h->stream));

@@ -10,6 +10,8 @@
 // no partial vectors, sigma written once with coalesced stores.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <set>
 #include <type_traits>
 #include <vector>
 
@@ -18,9 +20,40 @@
 
 namespace doci {
 
+#define DOCI_TRY_S(expr)            \
+  do {                              \
+    const int _st = (expr);         \
+    if (_st != DOCI_OK) return _st; \
+  } while (0)
+
 namespace {
 
 constexpr int kThreads = 256;
+
+// Launch configuration shared by the dynamic-shared-memory kernels: the
+// attribute is raised once per kernel to the largest size any handle uses
+// (under a lock: solves run concurrently from several host threads), and the
+// resident blocks per SM are queried per launch (a host-side computation).
+constexpr int kMaxDynSmem = 215 * 1024;
+std::mutex g_attr_mu;
+std::set<const void *> g_attr_done;
+
+template <typename KernelT>
+int blocks_for(KernelT kern, int threads, size_t dyn, int *blocks) {
+  {
+    std::lock_guard<std::mutex> lock(g_attr_mu);
+    const void *key = reinterpret_cast<const void *>(kern);
+    if (!g_attr_done.count(key)) {
+      DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
+      g_attr_done.insert(key);
+    }
+  }
+  int b = 0;
+  DOCI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, threads, dyn));
+  *blocks = b < 1 ? 1 : b;
+  return DOCI_OK;
+}
+
 
 struct SigmaShape {
   uint32_t D;
@@ -68,11 +101,8 @@ sigma_gather_kernel(SigmaShape s, const uint32_t *__restrict__ g_binom, const Re
 template <typename Real, int NH>
 int launch_nh(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
   const SigmaShape s{h->D, h->L, h->N, h->nh};
-  static int blocks_per_sm = 0;
-  if (!blocks_per_sm) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, sigma_gather_kernel<Real, NH>, kThreads, 0);
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
-  }
+  int blocks_per_sm = 1;
+  DOCI_TRY_S(blocks_for(sigma_gather_kernel<Real, NH>, kThreads, 0, &blocks_per_sm));
   const uint64_t need = (static_cast<uint64_t>(h->D) + kThreads - 1) / kThreads;
   uint64_t grid = static_cast<uint64_t>(device_sm_count()) * blocks_per_sm;
   if (grid > need) grid = need;
@@ -288,15 +318,8 @@ int launch_row(const doci_ham *h, const void *x, void *y, cudaStream_t st, int w
   const RowShape s{h->D, h->L, h->N, h->split, h->L - h->split, h->nrows};
   const size_t dyn = static_cast<size_t>(h->max_row) * sizeof(Real);
   auto kern = sigma_row_kernel<Real, 16>;
-  static int blocks_per_sm = 0;
-  static size_t configured = 0;
-  if (configured != dyn) {
-    DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
-    blocks_per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kRowThreads, dyn);
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
-    configured = dyn;
-  }
+  int blocks_per_sm = 1;
+  DOCI_TRY_S(blocks_for(kern, kRowThreads, dyn, &blocks_per_sm));
   int grid = device_sm_count() * blocks_per_sm;
   if (grid > h->nrows) grid = h->nrows;
   const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
@@ -494,14 +517,8 @@ int launch_rowx(const doci_ham *h, const void *x, void *y, cudaStream_t st, int 
   const uint32_t pad = (static_cast<uint32_t>(h->max_row) + 3u) & ~3u;
   const size_t dyn = 2 * static_cast<size_t>(pad) * sizeof(Real);
   auto kern = sigma_rowx_kernel<Real, 16>;
-  static size_t configured = 0;
-  static int blocks_per_sm = 1;
-  if (configured != dyn) {
-    DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kRowxThreads, dyn);
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
-    configured = dyn;
-  }
+  int blocks_per_sm = 1;
+  DOCI_TRY_S(blocks_for(kern, kRowxThreads, dyn, &blocks_per_sm));
   int grid = device_sm_count() * blocks_per_sm;
   if (grid > h->nrows) grid = h->nrows;
   const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
@@ -615,16 +632,14 @@ int launch_col(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
   // the neighbour routine keeps one register slot per row-part hole
   const int kmin = h->N - h->split > 0 ? h->N - h->split : 0;
   const bool wide = s.na - kmin > 16;
-  auto kern = wide ? sigma_col_kernel<Real, W, 24> : sigma_col_kernel<Real, W, 16>;
-  static size_t configured[2] = {0, 0};
-  static int blocks_per_sm[2] = {1, 1};
-  if (configured[wide] != dyn) {
-    DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[wide], kern, kColThreads, dyn);
-    if (blocks_per_sm[wide] < 1) blocks_per_sm[wide] = 1;
-    configured[wide] = dyn;
+  int bps = 1;
+  if (wide) {
+    DOCI_TRY_S(blocks_for(sigma_col_kernel<Real, W, 24>, kColThreads, dyn, &bps));
+  } else {
+    DOCI_TRY_S(blocks_for(sigma_col_kernel<Real, W, 16>, kColThreads, dyn, &bps));
   }
-  int grid = device_sm_count() * blocks_per_sm[wide];
+  auto kern = wide ? sigma_col_kernel<Real, W, 24> : sigma_col_kernel<Real, W, 16>;
+  int grid = device_sm_count() * bps;
   if (grid > npanels) grid = npanels;
   const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
                                                    : reinterpret_cast<const Real *>(h->d_Kmir32);

@@ -23,17 +23,24 @@ namespace doci {
 
 namespace {
 
+// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync): freeing
+// does not synchronise the device, so concurrent solves on other streams keep
+// running.
 struct DevMem {
   void *p = nullptr;
+  cudaStream_t st = nullptr;
   DevMem() = default;
   DevMem(const DevMem &) = delete;
   DevMem &operator=(const DevMem &) = delete;
-  ~DevMem() { cudaFree(p); }
-  int alloc(size_t bytes) {
-    cudaFree(p);
+  ~DevMem() {
+    if (p) cudaFreeAsync(p, st);
+  }
+  int alloc(size_t bytes, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, st);
     p = nullptr;
+    st = s;
     if (bytes == 0) bytes = 16;
-    DOCI_CUDA(cudaMalloc(&p, bytes));
+    DOCI_CUDA(cudaMallocAsync(&p, bytes, s));
     return DOCI_OK;
   }
   template <typename T>
@@ -102,11 +109,11 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
   if (maxv < 2 || maxv > 32 || keep < 1 || keep >= maxv) return DOCI_ERR_INVALID;
   const int precision = sizeof(S) == 8 ? DOCI_FP64 : DOCI_FP32;
   DevMem V, VA, part, small;
-  DOCI_TRY(V.alloc(sizeof(S) * D * maxv));
-  DOCI_TRY(VA.alloc(sizeof(S) * D * maxv));
-  DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity()));
+  DOCI_TRY(V.alloc(sizeof(S) * D * maxv, st));
+  DOCI_TRY(VA.alloc(sizeof(S) * D * maxv, st));
+  DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity(), st));
   // small device scratch: [0,64) reduction output, [64,96) y/c, [96, 96+32*32) Y
-  DOCI_TRY(small.alloc(sizeof(double) * (96 + 32 * 32)));
+  DOCI_TRY(small.alloc(sizeof(double) * (96 + 32 * 32), st));
   double *d_red = small.as<double>(), *d_vec = d_red + 64, *d_Y = d_red + 96;
   S *Vp = V.as<S>(), *VAp = VA.as<S>();
   double *dp = part.as<double>();
@@ -226,13 +233,162 @@ template int davidson_run<double>(MatvecOp &, size_t, const double *, double *, 
 template int davidson_run<float>(MatvecOp &, size_t, const double *, float *, const DavidsonArgs &, cudaStream_t,
                                  DavidsonOut *, double *);
 
+
+// ---------------------------------------------------------------------------
+// Block Davidson (nroots lowest eigenpairs).  Each iteration appends the
+// preconditioned residuals of the unconverged roots, each orthogonalised by
+// classical Gram-Schmidt twice against the whole basis (skipped if it has no
+// component left), computes their sigmas and the new subspace columns, and
+// re-diagonalises; the basis restarts from the `keep` lowest Ritz vectors
+// when the next block would not fit.
+// ---------------------------------------------------------------------------
+template <typename S>
+int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, const BlockArgs &a, cudaStream_t st,
+                       BlockOut *out, double *d_X_out) {
+  const int R = a.nroots, maxv = a.max_vectors;
+  const int keep = a.keep > R ? a.keep : R;
+  if (R < 1 || R > 8 || maxv > 32 || maxv < keep + R) return DOCI_ERR_INVALID;
+  const int precision = sizeof(S) == 8 ? DOCI_FP64 : DOCI_FP32;
+  DevMem V, VA, part, small, tbuf;
+  DOCI_TRY(V.alloc(sizeof(S) * D * maxv, st));
+  DOCI_TRY(VA.alloc(sizeof(S) * D * maxv, st));
+  DOCI_TRY(tbuf.alloc(sizeof(S) * D * R, st));
+  DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity(), st));
+  DOCI_TRY(small.alloc(sizeof(double) * (96 + 32 * 32), st));
+  double *d_red = small.as<double>(), *d_vec = d_red + 64, *d_Y = d_red + 96;
+  S *Vp = V.as<S>(), *VAp = VA.as<S>(), *Tp = tbuf.as<S>();
+  double *dp = part.as<double>();
+  std::vector<double> Sm(maxv * maxv, 0.0), Y(maxv * maxv, 0.0), w(maxv, 0.0), red(64);
+  auto fetch = [&](int nk) -> int {
+    DOCI_TRY(vec_reduce(dp, nk, d_red, st));
+    DOCI_CUDA(cudaMemcpyAsync(red.data(), d_red, sizeof(double) * nk, cudaMemcpyDeviceToHost, st));
+    DOCI_CUDA(cudaStreamSynchronize(st));
+    return DOCI_OK;
+  };
+  // append the vector in `t` (orthonormalised against V_0..V_{m-1}); returns
+  // false when nothing independent is left
+  int m = 0;
+  auto append = [&](S *t, bool *added) -> int {
+    *added = false;
+    double n0;
+    DOCI_TRY(vec_multidot<S>(t, D, 1, t, D, dp, st));
+    DOCI_TRY(fetch(1));
+    n0 = red[0];
+    if (!(n0 > 0)) return DOCI_OK;
+    std::vector<double> c(32, 0.0);
+    if (m > 0) {
+      for (int pass = 0; pass < 2; ++pass) {
+        DOCI_TRY(vec_multidot<S>(Vp, D, m, t, D, dp, st));
+        DOCI_TRY(fetch(m));
+        for (int i = 0; i < m; ++i) c[i] = red[i];
+        DOCI_CUDA(cudaMemcpyAsync(d_vec, c.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+        DOCI_TRY(vec_gs_update<S>(Vp, D, m, d_vec, D, t, dp, st));
+      }
+      DOCI_TRY(fetch(m + 1));
+    } else {
+      red[0] = n0;
+    }
+    const double n1 = red[0];
+    if (!(n1 > 1e-20 * n0) || !(n1 > 0)) return DOCI_OK;  // no independent direction left
+    DOCI_TRY(vec_gs_finish<S>(Vp, D, 0, nullptr, 1.0 / std::sqrt(n1), D, t, Vp + static_cast<size_t>(m) * D, dp, st));
+    DOCI_TRY(op.apply(Vp + static_cast<size_t>(m) * D, VAp + static_cast<size_t>(m) * D, precision, st));
+    out->sigmas++;
+    DOCI_TRY(vec_multidot<S>(Vp, D, m + 1, VAp + static_cast<size_t>(m) * D, D, dp, st));
+    DOCI_TRY(fetch(m + 1));
+    for (int i = 0; i <= m; ++i) Sm[m * maxv + i] = red[i];
+    ++m;
+    *added = true;
+    return DOCI_OK;
+  };
+
+  std::vector<int> active(R, 1);
+  std::vector<double> res(R, 1e300);
+  double best = 1e300;
+  int stall = 0, its = 0;
+  // start block
+  for (int r = 0; r < R; ++r) {
+    bool added;
+    DOCI_TRY(append(d_T + static_cast<size_t>(r) * D, &added));
+  }
+  if (m == 0) return DOCI_ERR_INVALID;
+  while (true) {
+    ++its;
+    jacobi_eig(m, Sm.data(), maxv, w.data(), Y.data());
+    const int nr = R < m ? R : m;
+    if (m + R > maxv) {  // thick restart to the `keep` lowest Ritz vectors
+      const int kk = keep < m ? keep : m;
+      DOCI_CUDA(cudaMemcpyAsync(d_Y, Y.data(), sizeof(double) * maxv * kk, cudaMemcpyHostToDevice, st));
+      DOCI_TRY(vec_deflate<S>(Vp, D, m, kk, d_Y, maxv, D, st));
+      DOCI_TRY(vec_deflate<S>(VAp, D, m, kk, d_Y, maxv, D, st));
+      for (int cc = 0; cc < kk; ++cc) {
+        DOCI_TRY(vec_multidot<S>(Vp, D, cc + 1, VAp + static_cast<size_t>(cc) * D, D, dp, st));
+        DOCI_TRY(fetch(cc + 1));
+        for (int i = 0; i <= cc; ++i) Sm[cc * maxv + i] = red[i];
+      }
+      m = kk;
+      jacobi_eig(m, Sm.data(), maxv, w.data(), Y.data());
+    }
+    // residuals and corrections of the unconverged roots
+    double worst = 0;
+    int nnew = 0;
+    for (int r = 0; r < nr; ++r) {
+      DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data() + static_cast<size_t>(r) * maxv, sizeof(double) * m,
+                                cudaMemcpyHostToDevice, st));
+      S *t = Tp + static_cast<size_t>(nnew) * D;
+      DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, w[r], d_diag, D, t, nullptr, dp, st));
+      DOCI_TRY(fetch(2));
+      res[r] = std::sqrt(red[0]);
+      worst = res[r] > worst ? res[r] : worst;
+      active[r] = res[r] > a.tol;
+      if (active[r]) ++nnew;
+    }
+    out->iterations = its;
+    if (worst <= a.tol || its >= a.max_its) break;
+    if (a.stall_window > 0) {
+      if (worst < best) {
+        best = worst;
+        stall = 0;
+      } else if (++stall >= a.stall_window) {
+        break;
+      }
+    }
+    int added_any = 0;
+    for (int q = 0; q < nnew; ++q) {
+      bool added;
+      DOCI_TRY(append(Tp + static_cast<size_t>(q) * D, &added));
+      added_any += added;
+    }
+    if (!added_any) break;
+  }
+  const int nr = R < m ? R : m;
+  for (int r = 0; r < nr; ++r) {
+    out->energy[r] = w[r];
+    out->residual[r] = res[r];
+    if (d_X_out) {
+      DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data() + static_cast<size_t>(r) * maxv, sizeof(double) * m,
+                                cudaMemcpyHostToDevice, st));
+      DOCI_TRY(vec_combine<S>(Vp, D, m, d_vec, D, d_X_out + static_cast<size_t>(r) * D, st));
+    }
+  }
+  double worst = 0;
+  for (int r = 0; r < nr; ++r) worst = res[r] > worst ? res[r] : worst;
+  out->converged = worst <= a.tol;
+  DOCI_CUDA(cudaStreamSynchronize(st));
+  return DOCI_OK;
+}
+
+template int block_davidson_run<double>(MatvecOp &, size_t, const double *, double *, const BlockArgs &, cudaStream_t,
+                                        BlockOut *, double *);
+template int block_davidson_run<float>(MatvecOp &, size_t, const double *, float *, const BlockArgs &, cudaStream_t,
+                                       BlockOut *, double *);
+
 // RQ-CG (CG.c:13-164).  d_x holds the start vector and receives the result.
 int ray_q_run(MatvecOp &op, size_t D, const double *d_diag_or_null, double *d_x, const CgArgs &a, cudaStream_t st,
               CgOut *out) {
   DevMem buf, part, small;
-  DOCI_TRY(buf.alloc(sizeof(double) * D * 5));
-  DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity()));
-  DOCI_TRY(small.alloc(sizeof(double) * 64));
+  DOCI_TRY(buf.alloc(sizeof(double) * D * 5, st));
+  DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity(), st));
+  DOCI_TRY(small.alloc(sizeof(double) * 64, st));
   double *p = buf.as<double>(), *Ax = p + D, *Ap = Ax + D, *g = Ap + D, *pinv = g + D;
   double *dp = part.as<double>(), *d_red = small.as<double>();
   double red[8];

@@ -61,6 +61,26 @@ struct CgOut {
 
 double now_s();  // steady clock, seconds
 
+struct BlockArgs {
+  int nroots = 1, max_vectors = 16, keep = 0, max_its = 200;
+  double tol = 1e-8;         // on every root's residual norm
+  int stall_window = 0;      // > 0: stop when the largest residual stops reaching new minima
+};
+
+struct BlockOut {
+  double energy[8] = {};
+  double residual[8] = {};
+  int iterations = 0, converged = 0, sigmas = 0;
+};
+
+// Block Davidson for the nroots lowest eigenpairs (no counterpart in the
+// reference, which is single-root).  d_T holds nroots start vectors (column-
+// major D x nroots, storage S); d_X_out (FP64, D x nroots) receives the Ritz
+// vectors.  diag is the FP64 diagonal (preconditioner |diag - theta|).
+template <typename S>
+int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, const BlockArgs &a, cudaStream_t st,
+                       BlockOut *out, double *d_X_out);
+
 template <typename S>
 int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const DavidsonArgs &a, cudaStream_t st,
                  DavidsonOut *out, double *d_x_out);

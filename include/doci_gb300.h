@@ -238,6 +238,61 @@ int doci_solve_trace(doci_ham *ham, const doci_solve_opts *opts, double *vec, do
 /* Bytes of device memory a solve of ham with opts needs (admission). */
 int64_t doci_solve_footprint(int L, int n_pairs, const doci_solve_opts *opts, int nroots);
 
+/* ------------------------------------------------------------------------ */
+/* Several roots, batched solves, request server.  No counterpart in the     */
+/* reference (single Hamiltonian, lowest root: davidson.c:90, :117).          */
+/* ------------------------------------------------------------------------ */
+
+typedef struct doci_batch_opts {
+  int nroots;          /* lowest eigenpairs per Hamiltonian, 1..8 (default 1) */
+  int max_vec;         /* block-Davidson basis size, >= 2 nroots, <= 32 (16) */
+  int max_its;         /* iteration limit (200) */
+  double tol;          /* residual-norm tolerance of every root (1e-6) */
+  int mode;            /* DOCI_MODE_MIXED (default) or DOCI_MODE_FP64 */
+  double mixed_tol;    /* residual at which the FP32 phase hands over (1e-4) */
+  int workers;         /* solves in flight at once, one CUDA stream each (8) */
+  int64_t hbm_budget;  /* device bytes the solves in flight may hold; 0 = 85% of free */
+} doci_batch_opts;
+
+typedef struct doci_root_result {
+  double energy[8];       /* lowest eigenvalues, ascending */
+  double residual[8];     /* final FP64 residual norms */
+  double energy_fp32[8];  /* energies at the end of the FP32 phase (mixed mode) */
+  int nroots, iterations, iterations_fp32, sigmas, converged;
+  int status;             /* doci_status of this solve */
+  double queued_s, start_s, end_s;  /* server clock: submitted, admitted, finished */
+} doci_root_result;
+
+void doci_batch_opts_default(doci_batch_opts *opts);
+
+/* Device bytes one solve of an (L, n_pairs) Hamiltonian holds (admission). */
+int64_t doci_roots_footprint(int L, int n_pairs, const doci_batch_opts *opts);
+
+/* Block-Davidson solve for the opts->nroots lowest eigenpairs (start vectors:
+ * unit vectors on the lowest diagonal elements); vecs (host, D x nroots,
+ * column-major) may be NULL. */
+int doci_solve_roots(doci_ham *ham, const doci_batch_opts *opts, doci_root_result *result, double *vecs);
+
+/* Solve many Hamiltonians: up to opts->workers solves in flight on their own
+ * streams, admitted against opts->hbm_budget.  results[i] for hams[i]. */
+int doci_batch_solve(int n, doci_ham *const *hams, const doci_batch_opts *opts, doci_root_result *results);
+
+/* Request server: submitted requests (integrals or an FCIDUMP path) are
+ * admitted as workers and memory free up, built on the device and solved
+ * concurrently (continuous batching).  Tickets identify requests. */
+typedef struct doci_server doci_server;
+int doci_server_create(const doci_batch_opts *opts, doci_server **out);
+int doci_server_submit(doci_server *srv, int L, int n_pairs, double core, const double *one, const double *two,
+                       int64_t *ticket);
+int doci_server_submit_fcidump(doci_server *srv, const char *path, int64_t *ticket);
+/* DOCI_ERR_PENDING while the request is queued or running */
+int doci_server_poll(doci_server *srv, int64_t ticket, doci_root_result *out);
+int doci_server_wait(doci_server *srv, int64_t ticket, doci_root_result *out);
+int doci_server_stats(doci_server *srv, int64_t *submitted, int64_t *finished, int64_t *running,
+                      int64_t *bytes_in_use);
+/* Finishes the queued requests, then stops the workers. */
+void doci_server_destroy(doci_server *srv);
+
 #ifdef __cplusplus
 }
 #endif
