@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <map>
 #include <set>
 #include <type_traits>
 #include <vector>
@@ -30,23 +31,31 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// Launch configuration shared by the dynamic-shared-memory kernels: the
-// attribute is raised once per kernel to the largest size any handle uses
-// (under a lock: solves run concurrently from several host threads), and the
-// resident blocks per SM are queried per launch (a host-side computation).
-constexpr int kMaxDynSmem = 215 * 1024;
+// Launch configuration shared by the dynamic-shared-memory kernels: once per
+// kernel (under a lock: solves run concurrently from several host threads)
+// the dynamic shared-memory limit is raised to what the device allows next to
+// the kernel's static shared memory; the resident blocks per SM are queried
+// per launch (a host-side computation).
 std::mutex g_attr_mu;
-std::set<const void *> g_attr_done;
+std::map<const void *, size_t> g_attr_limit;
 
 template <typename KernelT>
 int blocks_for(KernelT kern, int threads, size_t dyn, int *blocks) {
   {
     std::lock_guard<std::mutex> lock(g_attr_mu);
     const void *key = reinterpret_cast<const void *>(kern);
-    if (!g_attr_done.count(key)) {
-      DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
-      g_attr_done.insert(key);
+    auto it = g_attr_limit.find(key);
+    if (it == g_attr_limit.end()) {
+      int dev = 0, optin = 0;
+      DOCI_CUDA(cudaGetDevice(&dev));
+      DOCI_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+      cudaFuncAttributes fa;
+      DOCI_CUDA(cudaFuncGetAttributes(&fa, kern));
+      const size_t limit = static_cast<size_t>(optin) > fa.sharedSizeBytes ? optin - fa.sharedSizeBytes : 0;
+      DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(limit)));
+      it = g_attr_limit.emplace(key, limit).first;
     }
+    if (dyn > it->second) return DOCI_ERR_INVALID;
   }
   int b = 0;
   DOCI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, threads, dyn));
