@@ -336,7 +336,7 @@ int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, con
                                 cudaMemcpyHostToDevice, st));
       S *t = Tp + static_cast<size_t>(nnew) * D;
       DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, w[r], d_diag, D, t, nullptr, dp, st));
-      DOCI_TRY(fetch(2));
+      DOCI_TRY(fetch(m + 2));  // the residual pass writes m + 2 partials per block
       res[r] = std::sqrt(red[0]);
       worst = res[r] > worst ? res[r] : worst;
       active[r] = res[r] > a.tol;
