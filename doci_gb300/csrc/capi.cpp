@@ -475,7 +475,14 @@ struct SolverContext {
   cudaStream_t st = nullptr;
   cudaStream_t own = nullptr;
   ~SolverContext() {
-    if (own) cudaStreamDestroy(own);
+    // members are destroyed after this body: free the diagonal copy while its
+    // stream still exists, then retire the stream
+    if (diag_buf.p) cudaFreeAsync(diag_buf.p, diag_buf.st);
+    diag_buf.p = nullptr;
+    if (own) {
+      cudaStreamSynchronize(own);
+      cudaStreamDestroy(own);
+    }
   }
   int init(void (*matvec)(double *, double *, void *), void *vdat, const double *diagonal, size_t n) {
     op.n = n;
