@@ -58,6 +58,17 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge measurement")
+    ap.add_argument("--workload", choices=["sigma", "batch", "serve"], default="sigma",
+                    help="sigma: the headline sigma benchmark; batch: many Hamiltonians, several roots; "
+                         "serve: Poisson request stream through the request server")
+    ap.add_argument("--problems", type=int, default=256, help="batch: number of Hamiltonians")
+    ap.add_argument("--sequential-sample", type=int, default=64, help="batch: one-at-a-time baseline sample")
+    ap.add_argument("--roots", type=int, default=4)
+    ap.add_argument("--workers", type=int, default=16)
+    ap.add_argument("--requests", type=int, default=200, help="serve: number of requests")
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate, requests/s")
+    ap.add_argument("--lmin", type=int, default=None)
+    ap.add_argument("--lmax", type=int, default=None)
     ap.add_argument("--max-vec", type=int, default=16, help="DAVIDSON_MAX_VEC of the convergence runs")
     ap.add_argument("--mixed-tol", type=float, default=1e-5)
     return ap.parse_args()
@@ -231,11 +242,103 @@ def cpu_sample(path: str, seconds: float, seed: int = 0):
     return {"dets": n, "seconds": dt, "rate": n / dt, "threads": threads, "D": D, "run": run}
 
 
+def pct(v, q):
+    import numpy as np
+    return float(np.percentile(np.asarray(v), q)) if len(v) else None
+
+
+def batch_workload(a):
+    """Many seeded Hamiltonians (L uniform in [lmin, lmax], N = L // 2), the
+    `roots` lowest eigenpairs each, mixed precision; batched (workers solves
+    in flight) against one at a time (a sample)."""
+    import numpy as np
+    import doci_gb300 as dg
+    from doci_gb300.fcidump import raw_integrals
+    lmin, lmax = a.lmin or 12, a.lmax or 24
+    rng = np.random.default_rng(4)
+    Ls = rng.integers(lmin, lmax + 1, size=a.problems)
+    t0 = time.perf_counter()
+    hams = []
+    for i, L in enumerate(Ls):
+        one, two = raw_integrals(int(L), 1000 + i)
+        hams.append(dg.Hamiltonian.from_integrals(int(L), int(L) // 2, 0.0, one, two))
+    t_build = time.perf_counter() - t0
+    opts = dict(nroots=a.roots, tol=1e-5, mode="mixed", mixed_tol=1e-3, max_vec=max(16, 4 * a.roots))
+    k = min(a.sequential_sample, a.problems)
+    idx = np.linspace(0, a.problems - 1, k).astype(int)
+    t0 = time.perf_counter()
+    seq = [dg.solve_roots(hams[i], **opts) for i in idx]
+    t_seq = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    st, res = dg.batch_solve(hams, workers=a.workers, **opts)
+    t_bat = time.perf_counter() - t0
+    same = all(res[i]["energies"] == seq[j]["energies"] for j, i in enumerate(idx))
+    lat = [r["end_s"] - r["queued_s"] for r in res]
+    for h in hams:
+        h.close()
+    line = {"metric": "batched solves/s (4 lowest roots, mixed precision)", "value": round(a.problems / t_bat, 3),
+            "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "impl": "ours", "dtype": "f32+f64",
+            "data": "synthetic", "status": st, "one_at_a_time": round(k / t_seq, 3),
+            "speedup_vs_one_at_a_time": round((a.problems / t_bat) / (k / t_seq), 3),
+            "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99), "same_alone_and_in_batch": same,
+            "converged": int(sum(r["converged"] for r in res)), "build_s": round(t_build, 2),
+            "config": {"workload": f"{a.problems} Hamiltonians, L uniform in {lmin}..{lmax}, N=L//2, "
+                                   f"{a.roots} roots, workers={a.workers}", "opts": opts,
+                       "sequential_sample": k}}
+    print(json.dumps(line), flush=True)
+
+
+def serve_workload(a):
+    """Poisson request stream into the request server: per-request seeded
+    integrals, L uniform in [lmin, lmax], N = L // 2 + d, d uniform in -2..2."""
+    import numpy as np
+    import doci_gb300 as dg
+    from doci_gb300.fcidump import raw_integrals
+    lmin, lmax = a.lmin or 16, a.lmax or 24
+    rng = np.random.default_rng(7)
+    gaps = rng.exponential(1.0 / a.rate, size=a.requests)
+    reqs = []
+    for i in range(a.requests):
+        L = int(rng.integers(lmin, lmax + 1))
+        N = max(1, min(L - 1, L // 2 + int(rng.integers(-2, 3))))
+        one, two = raw_integrals(L, 2000 + i)
+        reqs.append((L, N, one, two))
+    tickets = []
+    with dg.Server(nroots=1, tol=1e-5, mode="mixed", mixed_tol=1e-3, workers=a.workers) as srv:
+        t0 = time.perf_counter()
+        at = 0.0
+        for (L, N, one, two), g in zip(reqs, gaps):
+            at += g
+            wait = at - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            tickets.append(srv.submit(L, N, one, two))
+        res = [srv.wait(t) for t in tickets]
+        span = time.perf_counter() - t0
+    lat = [r["end_s"] - r["queued_s"] for r in res]
+    dE = [abs(r["energies_fp32"][0] - r["energies"][0]) for r in res]
+    line = {"metric": "serving p50/p99 latency and solves/s (Poisson arrivals)", "value": round(a.requests / span, 3),
+            "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "impl": "ours", "dtype": "f32+f64",
+            "data": "synthetic", "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99),
+            "offered_rate": a.rate, "requests": a.requests,
+            "ok": int(sum(r["status"] == 0 for r in res)), "converged": int(sum(r["converged"] for r in res)),
+            "fp32_phase_dE_max_Ha": max(dE) if dE else None,
+            "note": "final energies are FP64-refined (FP64 block-Davidson phase to tol); fp32_phase_dE is "
+                    "|E(FP32 phase) - E(final)| per request",
+            "config": {"workload": f"{a.requests} requests, L uniform in {lmin}..{lmax}, N=L//2+-2, "
+                                   f"rate {a.rate}/s, workers={a.workers}"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
     ws, rank, local = dist_env()
     if a.impl == "reference":
         return reference_arm(a, ws, rank)
+    if a.workload == "batch":
+        return batch_workload(a)
+    if a.workload == "serve":
+        return serve_workload(a)
     import numpy as np
     import torch
     import doci_gb300 as dg

@@ -9,6 +9,8 @@
 
 #include <cstdlib>
 #include <algorithm>
+#include <array>
+#include <map>
 #include <mutex>
 #include <cstring>
 #include <utility>
@@ -54,7 +56,7 @@ void ham_release(doci_ham *h) {
   cudaStream_t st = h->stream;
   void *bufs[] = {h->d_binom, h->d_Kmir64, h->d_Kmir32, h->d_tab64, h->d_diag, h->d_diag32, h->d_stage_x,
                   h->d_stage_y, h->d_rows, h->d_rowstart, h->d_sector_rs, h->d_sector_off, h->d_panels[0],
-                  h->d_panels[1], h->d_rem, h->d_ins, h->d_tab_off};
+                  h->d_panels[1]};  // d_rem/d_ins/d_tab_off are shared (per-process cache)
   for (void *p : bufs) release_async(p, st);
   if (h->h_diag) cudaFreeHost(h->h_diag);
   if (st) {
@@ -249,17 +251,28 @@ int ham_build_rows(doci_ham *h) {
   DOCI_CUDA(cudaMemcpyAsync(h->d_rowstart, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                             h->stream));
   {
-    std::vector<uint32_t> B(kBinomRows * kBinomCols), rem, ins, toff;
-    fill_binom_table(B.data());
-    dev::build_cross_tables(split, B.data(), kBinomCols, rem, ins, toff);
-    DOCI_CUDA(cudaMallocAsync(&h->d_rem, rem.size() * sizeof(uint32_t), h->stream));
-    DOCI_CUDA(cudaMallocAsync(&h->d_ins, ins.size() * sizeof(uint32_t), h->stream));
-    DOCI_CUDA(cudaMallocAsync(&h->d_tab_off, toff.size() * sizeof(uint32_t), h->stream));
-    DOCI_CUDA(cudaMemcpyAsync(h->d_rem, rem.data(), rem.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    DOCI_CUDA(cudaMemcpyAsync(h->d_ins, ins.data(), ins.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    DOCI_CUDA(cudaMemcpyAsync(h->d_tab_off, toff.data(), toff.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                              h->stream));
-    DOCI_CUDA(cudaStreamSynchronize(h->stream));
+    // cross-hop tables depend only on (device, split): built once per process
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, std::array<uint32_t *, 3>> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(h->device, split);
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+      std::vector<uint32_t> B(kBinomRows * kBinomCols), rem, ins, toff;
+      fill_binom_table(B.data());
+      dev::build_cross_tables(split, B.data(), kBinomCols, rem, ins, toff);
+      std::array<uint32_t *, 3> t{};
+      DOCI_CUDA(cudaMalloc(&t[0], rem.size() * sizeof(uint32_t)));
+      DOCI_CUDA(cudaMalloc(&t[1], ins.size() * sizeof(uint32_t)));
+      DOCI_CUDA(cudaMalloc(&t[2], toff.size() * sizeof(uint32_t)));
+      DOCI_CUDA(cudaMemcpy(t[0], rem.data(), rem.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+      DOCI_CUDA(cudaMemcpy(t[1], ins.data(), ins.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+      DOCI_CUDA(cudaMemcpy(t[2], toff.data(), toff.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+      it = cache.emplace(key, t).first;
+    }
+    h->d_rem = it->second[0];
+    h->d_ins = it->second[1];
+    h->d_tab_off = it->second[2];
   }
   DOCI_CUDA(cudaMallocAsync(&h->d_sector_off, sizeof(h->sector_off), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_sector_off, h->sector_off, sizeof(h->sector_off), cudaMemcpyHostToDevice, h->stream));
