@@ -52,7 +52,9 @@ def parse():
     ap.add_argument("--N", type=int, default=16)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
-    ap.add_argument("--kernel", choices=["auto", "gather", "row", "row1", "rowx", "rowxc"], default="auto")
+    ap.add_argument("--kernel", choices=["auto", "gather", "row", "row1", "rowx", "rowxc", "pair"], default="auto")
+    ap.add_argument("--block", type=int, default=1,
+                    help="sigma: vectors per step through doci_sigma_block (1 = doci_sigma)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -356,15 +358,24 @@ def main():
     h.set_sigma_kernel(a.kernel)
     D = h.D
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
-    x = torch.randn(D, dtype=tdt, device="cuda", generator=g)
+    nv = max(1, a.block)
+    x = torch.randn(D * nv, dtype=tdt, device="cuda", generator=g)
     y = torch.empty_like(x)
     torch.cuda.synchronize()
+    if nv > 1:  # a block of vectors per step: the device-timed figure only
+        a.no_e2e = a.no_converge = True
+
+    def step():
+        if nv == 1:
+            h.sigma_device(x.data_ptr(), y.data_ptr(), prec, sptr)
+        else:
+            h.sigma_block_device(x.data_ptr(), D, y.data_ptr(), D, nv, prec, sptr)
     # a dedicated stream: the sigma launches and the CUDA events share it
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
     assert sptr != 0
     for _ in range(a.warmup):
-        h.sigma_device(x.data_ptr(), y.data_ptr(), prec, sptr)
+        step()
     torch.cuda.synchronize()
     uuid = None
     try:
@@ -379,7 +390,7 @@ def main():
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps + 1)]
     ev[0].record(stream)
     for k in range(a.steps):
-        h.sigma_device(x.data_ptr(), y.data_ptr(), prec, sptr)
+        step()
         ev[k + 1].record(stream)
     torch.cuda.synchronize()
     if ws > 1:
@@ -387,9 +398,9 @@ def main():
     clk = clocks.stop()
     per_launch = [ev[k].elapsed_time(ev[k + 1]) * 1e-3 for k in range(a.steps)]
     total = max_over_ranks(ev[0].elapsed_time(ev[a.steps]) * 1e-3, ws)
-    value = replica_gdets(D, a.steps, ws, total)
+    value = replica_gdets(D * nv, a.steps, ws, total)
     mean_launch = statistics.mean(per_launch)
-    bytes_alg = D * (esize + esize + esize)  # x, diagonal, sigma
+    bytes_alg = D * (2 * nv + 1) * esize  # x and sigma per vector, the diagonal once
     peaks, peak_kind = measured_peaks()
     achieved = bytes_alg / mean_launch / 1e9
     traffic = None
@@ -400,7 +411,7 @@ def main():
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                "bytes_per_det": 3 * esize, "mean_launch_ms": round(mean_launch * 1e3, 4)}
+                "bytes_per_det": (2 * nv + 1) * esize, "mean_launch_ms": round(mean_launch * 1e3, 4)}
     e2e = None
     if not a.no_e2e:
         hx = torch.randn(D, dtype=tdt, generator=torch.Generator().manual_seed(5)).pin_memory()
@@ -435,11 +446,13 @@ def main():
                 "warmup": a.warmup, "ms_per_step": round(total / a.steps * 1e3, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == dg.FP32 else "f64",
                 "data": "synthetic (seeded FCIDUMP of the benchmark integral model)",
-                "config": {"workload": f"DOCI sigma L={a.L} N={a.N} D={D} seed={a.seed} {a.precision}",
+                "config": {"workload": f"DOCI sigma L={a.L} N={a.N} D={D} seed={a.seed} {a.precision}"
+                                       + (f" block of {nv} vectors" if nv > 1 else ""),
+                           "block": nv,
                            "L": a.L, "N": a.N, "D": D, "seed": a.seed, "precision": a.precision,
                            "l2": "inputs larger than L2 (x and sigma are D*4 B = %.2f GB each)" % (D * esize / 1e9),
                            "parallelism": f"replicas x{ws}"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": a.steps,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": a.steps * ((nv + 3) // 4),
                 "clocks": clk, "time_to_converge": conv, "impl": "ours"}
         print(json.dumps(line), flush=True)
     h.close()

@@ -100,6 +100,7 @@ def lib() -> C.CDLL:
         "doci_ham_diagonal": (i, [vp, pd]),
         "doci_ham_diagonal_device": (vp, [vp]),
         "doci_sigma": (i, [vp, vp, vp, i, vp]),
+        "doci_sigma_block": (i, [vp, vp, C.c_int64, vp, C.c_int64, i, i, vp]),
         "doci_sigma_host": (i, [vp, vp, vp, i]),
         "doci_ham_set_sigma_kernel": (i, [vp, i]),
         "doci_bitstrings": (i, [vp, i64, i64, vp, vp]),
@@ -208,7 +209,7 @@ class Hamiltonian:
 
     def set_sigma_kernel(self, kind) -> None:
         """0/'auto', 1/'gather', 2/'row' (row + column-panel passes), 3/'row1' (row pass only)."""
-        kind = {"auto": 0, "gather": 1, "row": 2, "row1": 3, "rowx": 4, "rowxc": 5}.get(kind, kind)
+        kind = {"auto": 0, "gather": 1, "row": 2, "row1": 3, "rowx": 4, "rowxc": 5, "pair": 6}.get(kind, kind)
         _check(lib().doci_ham_set_sigma_kernel(self._h, int(kind)), "doci_ham_set_sigma_kernel")
 
     def diagonal(self) -> np.ndarray:
@@ -233,6 +234,12 @@ class Hamiltonian:
         """sigma on device buffers (e.g. torch tensors' data_ptr())."""
         _check(lib().doci_sigma(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), precision,
                                 C.c_void_p(stream or None)), "doci_sigma")
+
+    def sigma_block_device(self, x_ptr: int, ldx: int, y_ptr: int, ldy: int, nv: int, precision: int = FP64,
+                           stream: int = 0) -> None:
+        """Block sigma over nv column-major vectors on device buffers."""
+        _check(lib().doci_sigma_block(self._h, C.c_void_p(x_ptr), ldx, C.c_void_p(y_ptr), ldy, nv, precision,
+                                      C.c_void_p(stream or None)), "doci_sigma_block")
 
     def bitstrings_device(self, first: int, count: int, out_ptr: int, stream: int = 0) -> None:
         _check(lib().doci_bitstrings(self._h, first, count, C.c_void_p(out_ptr), C.c_void_p(stream or None)),

@@ -172,8 +172,29 @@ int doci_sigma(doci_ham *h, const void *d_x, void *d_y, int precision, void *str
   return launch_sigma(h, d_x, d_y, precision, pick(h, stream));
 }
 
+int doci_sigma_block(doci_ham *h, const void *d_X, int64_t ldx, void *d_Y, int64_t ldy, int nv, int precision,
+                     void *stream) {
+  if (!h || !d_X || !d_Y || nv < 1 || ldx < h->D || ldy < h->D) return DOCI_ERR_INVALID;
+  if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
+  const size_t es = precision == DOCI_FP64 ? 8 : 4;
+  const char *x = static_cast<const char *>(d_X);
+  char *y = static_cast<char *>(d_Y);
+  // the output block must not overlap the input block
+  const char *xe = x + ((nv - 1) * static_cast<size_t>(ldx) + h->D) * es;
+  const char *ye = y + ((nv - 1) * static_cast<size_t>(ldy) + h->D) * es;
+  if (x < ye && y < xe) return DOCI_ERR_INVALID;
+  const cudaStream_t st = pick(h, stream);
+  for (int v0 = 0; v0 < nv; v0 += 4) {
+    const int k = nv - v0 < 4 ? nv - v0 : 4;
+    const int r = launch_sigma_multi(h, x + v0 * static_cast<size_t>(ldx) * es, ldx,
+                                     y + v0 * static_cast<size_t>(ldy) * es, ldy, k, precision, st);
+    if (r != DOCI_OK) return r;
+  }
+  return DOCI_OK;
+}
+
 int doci_ham_set_sigma_kernel(doci_ham *h, int kind) {
-  if (!h || kind < 0 || kind > 5) return DOCI_ERR_INVALID;
+  if (!h || kind < 0 || kind > 6) return DOCI_ERR_INVALID;
   h->sigma_kernel = kind;
   return DOCI_OK;
 }

@@ -56,7 +56,7 @@ void ham_release(doci_ham *h) {
   cudaStream_t st = h->stream;
   void *bufs[] = {h->d_binom, h->d_Kmir64, h->d_Kmir32, h->d_tab64, h->d_diag, h->d_diag32, h->d_stage_x,
                   h->d_stage_y, h->d_rows, h->d_rowstart, h->d_sector_rs, h->d_sector_off, h->d_panels[0],
-                  h->d_panels[1]};  // d_rem/d_ins/d_tab_off are shared (per-process cache)
+                  h->d_panels[1], h->d_pblocks, h->d_kfrag};  // d_rem/d_ins/d_tab_off are shared (per-process cache)
   for (void *p : bufs) release_async(p, st);
   if (h->h_diag) cudaFreeHost(h->h_diag);
   if (st) {
@@ -70,6 +70,8 @@ void ham_release(doci_ham *h) {
   h->d_rows = h->d_rowstart = h->d_sector_rs = nullptr;
   h->d_sector_off = nullptr;
   h->d_panels[0] = h->d_panels[1] = nullptr;
+  h->d_pblocks = h->d_kfrag = nullptr;
+  h->npblocks = 0;
   h->d_rem = h->d_ins = h->d_tab_off = nullptr;
   h->h_diag = nullptr;
   h->stream = nullptr;
@@ -294,7 +296,7 @@ int ham_build_rows(doci_ham *h) {
   DOCI_CUDA(cudaMemcpyAsync(h->d_sector_rs, sector.data(), sector.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                             h->stream));
   DOCI_CUDA(cudaStreamSynchronize(h->stream));
-  return DOCI_OK;
+  return ham_build_pairs(h, start);
 }
 
 }  // namespace doci

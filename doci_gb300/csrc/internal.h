@@ -95,6 +95,12 @@ struct doci_ham {
   // cross-hop index tables of the phase-ordered row pass (addressing.cuh,
   // build_cross_tables)
   uint32_t *d_rem = nullptr, *d_ins = nullptr, *d_tab_off = nullptr;
+  // pair form (sigma_pair.cu): one block per (N-1)-pair set's row part R',
+  // {own row start or ~0, mask | k' << 24}, largest first; the K matrix split
+  // into TF32 high and low parts in mma fragment order
+  uint32_t *d_pblocks = nullptr;
+  int npblocks = 0;
+  uint32_t *d_kfrag = nullptr;
 
   // host diagonal for doci_get_diagonal (lazy)
   double *h_diag = nullptr;
@@ -112,6 +118,16 @@ void ham_release(doci_ham *h);
 int ham_stage(doci_ham *h, size_t bytes);
 // sigma.cu
 int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t s);
+// nv <= 4 vectors x + v ldx -> y + v ldy with the neighbour work shared
+int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv, int precision,
+                       cudaStream_t s);
+// resident blocks per SM of a kernel with `dyn` bytes of dynamic shared
+// memory (raises the kernel's dynamic shared-memory limit on first use)
+int kernel_blocks(const void *kernel, int threads, size_t dyn, int *blocks);
+// pair-form sigma (sigma_pair.cu), FP32 only
+bool pair_fits(const doci_ham *h);
+int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t s);
+int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &row_start);
 int launch_bitstrings(const doci_ham *h, int64_t first, int64_t count, uint32_t *out, cudaStream_t s);
 int launch_ranks(const doci_ham *h, const uint32_t *bits, int64_t count, int64_t *out, cudaStream_t s);
 int launch_diagonal(doci_ham *h, cudaStream_t s);

@@ -41,28 +41,34 @@ std::map<const void *, size_t> g_attr_limit;
 
 template <typename KernelT>
 int blocks_for(KernelT kern, int threads, size_t dyn, int *blocks) {
+  return kernel_blocks(reinterpret_cast<const void *>(kern), threads, dyn, blocks);
+}
+
+}  // namespace
+
+int kernel_blocks(const void *key, int threads, size_t dyn, int *blocks) {
   {
     std::lock_guard<std::mutex> lock(g_attr_mu);
-    const void *key = reinterpret_cast<const void *>(kern);
     auto it = g_attr_limit.find(key);
     if (it == g_attr_limit.end()) {
       int dev = 0, optin = 0;
       DOCI_CUDA(cudaGetDevice(&dev));
       DOCI_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
       cudaFuncAttributes fa;
-      DOCI_CUDA(cudaFuncGetAttributes(&fa, kern));
+      DOCI_CUDA(cudaFuncGetAttributes(&fa, key));
       const size_t limit = static_cast<size_t>(optin) > fa.sharedSizeBytes ? optin - fa.sharedSizeBytes : 0;
-      DOCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(limit)));
+      DOCI_CUDA(cudaFuncSetAttribute(key, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(limit)));
       it = g_attr_limit.emplace(key, limit).first;
     }
     if (dyn > it->second) return DOCI_ERR_INVALID;
   }
   int b = 0;
-  DOCI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, threads, dyn));
+  DOCI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, key, threads, dyn));
   *blocks = b < 1 ? 1 : b;
   return DOCI_OK;
 }
 
+namespace {
 
 struct SigmaShape {
   uint32_t D;
@@ -137,6 +143,79 @@ int launch_typed(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
   if (nh <= 24) return launch_nh<Real, 24>(h, x, y, st);
   if (nh <= 28) return launch_nh<Real, 28>(h, x, y, st);
   return launch_nh<Real, 32>(h, x, y, st);
+}
+
+// Several vectors at once (block methods): x_v = x + v ldx, y_v = y + v ldy,
+// v < nv <= NV.  The unrank, neighbour ranks and weights are computed once
+// per determinant and hop and applied to every vector.
+template <typename Real, int NH, int NV>
+__global__ void __launch_bounds__(kThreads)
+sigma_gather_multi_kernel(SigmaShape s, const uint32_t *__restrict__ g_binom, const Real *__restrict__ g_K,
+                          const Real *__restrict__ diag, const Real *__restrict__ x, size_t ldx,
+                          Real *__restrict__ y, size_t ldy, int nv) {
+  __shared__ SigmaSmem<Real> sm;
+  for (int t = threadIdx.x; t < kBinomRows * kBinomCols; t += blockDim.x) sm.binom[t] = g_binom[t];
+  for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) sm.K[t] = g_K[t];
+  __syncthreads();
+  const uint32_t *B = sm.binom;
+  const uint32_t Dm1 = s.D - 1;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < s.D; r += gridDim.x * blockDim.x) {
+    const uint32_t R = Dm1 - r;
+    const uint32_t M = dev::colex_unrank<kBinomCols>(R, s.L, s.N, B);
+    dev::Neighbours<NH, kBinomCols> nb;
+    nb.precompute(M, R, s.L, s.nh, B);
+    struct Acc {
+      const Real *K, *x;
+      size_t ldx;
+      int nv;
+      const Real *Krow;
+      Real acc[NV];
+      __device__ __forceinline__ void begin(int m) { Krow = K + m * 32; }
+      __device__ __forceinline__ void hop(int, int q, uint32_t idx) {
+        const Real kv = Krow[q];
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          if (v < nv) acc[v] += kv * __ldg(x + v * ldx + idx);
+      }
+    } f{sm.K, x, ldx, nv, sm.K, {}};
+    const Real d = diag[r];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      if (v < nv) f.acc[v] = d * x[v * ldx + r];
+    nb.visit(M, R, Dm1, s.N, s.nh, B, f);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      if (v < nv) y[v * ldy + r] = f.acc[v];
+  }
+}
+
+template <typename Real, int NH>
+int launch_gather_multi(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv, cudaStream_t st) {
+  const SigmaShape s{h->D, h->L, h->N, h->nh};
+  int blocks_per_sm = 1;
+  DOCI_TRY_S(blocks_for(sigma_gather_multi_kernel<Real, NH, 4>, kThreads, 0, &blocks_per_sm));
+  const uint64_t need = (static_cast<uint64_t>(h->D) + kThreads - 1) / kThreads;
+  uint64_t grid = static_cast<uint64_t>(device_sm_count()) * blocks_per_sm;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
+                                                   : reinterpret_cast<const Real *>(h->d_Kmir32);
+  const Real *dg = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_diag)
+                                                    : reinterpret_cast<const Real *>(h->d_diag32);
+  sigma_gather_multi_kernel<Real, NH, 4><<<static_cast<unsigned>(grid), kThreads, 0, st>>>(
+      s, h->d_binom, K, dg, static_cast<const Real *>(x), ldx, static_cast<Real *>(y), ldy, nv);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+template <typename Real>
+int launch_gather_multi_typed(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv,
+                              cudaStream_t st) {
+  const int nh = h->nh;
+  if (nh <= 8) return launch_gather_multi<Real, 8>(h, x, ldx, y, ldy, nv, st);
+  if (nh <= 16) return launch_gather_multi<Real, 16>(h, x, ldx, y, ldy, nv, st);
+  if (nh <= 24) return launch_gather_multi<Real, 24>(h, x, ldx, y, ldy, nv, st);
+  return launch_gather_multi<Real, 32>(h, x, ldx, y, ldy, nv, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -320,6 +399,134 @@ sigma_row_kernel(RowShape s, int with_across, const uint2 *__restrict__ rows, co
       y[rstart + c] = f.acc;
     }
   }
+}
+
+template <typename Real, int NHB, int NV>
+__global__ void __launch_bounds__(kRowThreads, 2)
+sigma_row_multi_kernel(RowShape s, int nv, size_t ldx, size_t ldy, uint32_t row_pad, const uint2 *__restrict__ rows, const uint32_t *__restrict__ rowstart_of,
+                 const uint32_t *__restrict__ g_binom, const Real *__restrict__ g_K, const Real *__restrict__ diag,
+                 const Real *__restrict__ x, Real *__restrict__ y) {
+  __shared__ RowTables<Real> tb;
+  extern __shared__ __align__(16) unsigned char row_smem[];
+  Real *xs = reinterpret_cast<Real *>(row_smem);
+  for (int t = threadIdx.x; t < kBinomRows * kBinomCols; t += blockDim.x) tb.binom[t] = g_binom[t];
+  for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) tb.K[t] = g_K[t];
+  const uint32_t *B = tb.binom;
+  const int sp = s.split, na = s.na;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  for (int row = blockIdx.x; row < s.nrows; row += gridDim.x) {
+    const uint2 rw = rows[row];
+    const uint32_t rstart = rw.x, mask = rw.y & 0xffffffu;
+    const int k = static_cast<int>(rw.y >> 24), j = s.N - k;
+    __syncthreads();  // previous row finished with xs and the tables
+    if (warp == 0) {
+      // row-part elements and holes, compacted with ballots
+      const bool live = lane < na;
+      const bool in_r = live && ((mask >> lane) & 1u);
+      const bool hole = live && !in_r;
+      const uint32_t eb = __ballot_sync(0xffffffffu, in_r), hb = __ballot_sync(0xffffffffu, hole);
+      const uint32_t below = (1u << lane) - 1u;
+      if (in_r) {
+        const int e = __popc(eb & below);
+        tb.ab_rs[e] = rowstart_of[mask & ~(1u << lane)];
+        tb.ab_m[e] = sp + lane;
+      }
+      if (hole) {
+        const int h = __popc(hb & below);
+        tb.ba_rs[h] = rowstart_of[mask | (1u << lane)];
+        tb.ba_q[h] = sp + lane;
+      }
+      const int ne = __popc(eb), nhl = __popc(hb);
+      if (lane == 0) {
+        tb.n_ab = j < sp ? ne : 0;   // a column-part hole must exist
+        tb.n_ba = j > 0 ? nhl : 0;   // a column-part element must exist
+        tb.n_aa = ne * nhl;
+      }
+      // row part -> row part pairs (element e, hole h)
+      for (int t = lane; t < ne * nhl; t += 32) {
+        const int e = t / nhl, h = t % nhl;
+        const int a_e = __fns(eb, 0, e + 1), a_h = __fns(hb, 0, h + 1);
+        tb.aa_rs[t] = rowstart_of[(mask & ~(1u << a_e)) | (1u << a_h)];
+        tb.aa_K[t] = g_K[(sp + a_e) * 32 + sp + a_h];
+      }
+    }
+    const uint32_t n = B[sp * kBinomCols + j];
+    for (int v = 0; v < nv; ++v)
+      for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) xs[v * row_pad + c] = x[v * ldx + rstart + c];
+    __syncthreads();
+
+    const int n_aa = tb.n_aa, n_ab = tb.n_ab, n_ba = tb.n_ba;
+    struct Acc {
+      const RowTables<Real> &tb;
+      const Real *xs, *x;
+      size_t ldx;
+      uint32_t pad;
+      int nv;
+      const Real *Krow;
+      Real acc[NV];
+      __device__ __forceinline__ void begin(int m) { Krow = tb.K + m * 32; }
+      __device__ __forceinline__ void inrow(int, int q, uint32_t cc) {
+        const Real kv = Krow[q];
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          if (v < nv) acc[v] += kv * xs[v * pad + cc];
+      }
+      __device__ __forceinline__ void down(int t, int, int q, uint32_t cc) {
+        const Real kv = Krow[q];
+        const Real *src = x + tb.ba_rs[t] + cc;
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          if (v < nv) acc[v] += kv * __ldg(src + v * ldx);
+      }
+      __device__ __forceinline__ void up(int t, int m, int q, uint32_t cc) {
+        const Real kv = tb.K[m * 32 + q];
+        const Real *src = x + tb.ab_rs[t] + cc;
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          if (v < nv) acc[v] += kv * __ldg(src + v * ldx);
+      }
+      __device__ __forceinline__ void across(int t, uint32_t cc) {
+        const Real kv = tb.aa_K[t];
+        const Real *src = x + tb.aa_rs[t] + cc;
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          if (v < nv) acc[v] += kv * __ldg(src + v * ldx);
+      }
+    };
+    for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) {
+      Acc f{tb, xs, x, ldx, row_pad, nv, tb.K, {}};
+      const Real d = diag[rstart + c];
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        if (v < nv) f.acc[v] = d * xs[v * row_pad + c];
+      dev::row_column_hops<NHB, kBinomCols>(c, n, sp, j, B, n_ab, tb.ab_m, n_ba, tb.ba_q, n_aa, f);
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        if (v < nv) y[v * ldy + rstart + c] = f.acc[v];
+    }
+  }
+}
+
+
+template <typename Real>
+int launch_row_multi(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv, cudaStream_t st) {
+  const RowShape s{h->D, h->L, h->N, h->split, h->L - h->split, h->nrows};
+  const uint32_t pad = (static_cast<uint32_t>(h->max_row) + 3u) & ~3u;
+  const size_t dyn = static_cast<size_t>(nv) * pad * sizeof(Real);
+  int blocks_per_sm = 1;
+  DOCI_TRY_S(blocks_for(sigma_row_multi_kernel<Real, 16, 4>, kRowThreads, dyn, &blocks_per_sm));
+  int grid = device_sm_count() * blocks_per_sm;
+  if (grid > h->nrows) grid = h->nrows;
+  const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
+                                                   : reinterpret_cast<const Real *>(h->d_Kmir32);
+  const Real *dg = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_diag)
+                                                    : reinterpret_cast<const Real *>(h->d_diag32);
+  sigma_row_multi_kernel<Real, 16, 4><<<grid, kRowThreads, dyn, st>>>(
+      s, nv, ldx, ldy, pad, reinterpret_cast<const uint2 *>(h->d_rows), h->d_rowstart, h->d_binom, K, dg,
+      static_cast<const Real *>(x), static_cast<Real *>(y));
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
 }
 
 template <typename Real>
@@ -677,6 +884,9 @@ unsigned grid_for(uint64_t n) {
 int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t st) {
   if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
   const size_t elem = precision == DOCI_FP64 ? 8 : 4;
+  // pair form on request (kind 6, FP32 only)
+  if (h->sigma_kernel == 6 && precision == DOCI_FP32 && pair_fits(h))
+    return launch_pair(h, static_cast<const float *>(x), static_cast<float *>(y), st);
   // row kernel when the row tiling exists, fits, and gives every SM work
   bool row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
@@ -699,6 +909,45 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
                                  : launch_row<float>(h, x, y, st, col ? 0 : 1);
   if (r || !col) return r;
   return precision == DOCI_FP64 ? launch_col<double>(h, x, y, st) : launch_col<float>(h, x, y, st);
+}
+
+int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv, int precision,
+                       cudaStream_t st) {
+  if (nv < 1 || nv > 4 || ldx < h->D || ldy < h->D) return DOCI_ERR_INVALID;
+  if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
+  const size_t elem = precision == DOCI_FP64 ? 8 : 4;
+  if (nv == 1) return launch_sigma(h, x, y, precision, st);
+  const char *xc = static_cast<const char *>(x);
+  char *yc = static_cast<char *>(y);
+  // row pass: every vector's row staged in shared memory, so the group size
+  // is what fits beside the static tables (at most 212 KB of rows)
+  const size_t row_bytes = static_cast<size_t>((h->max_row + 3) & ~3) * elem;
+  const int fit = static_cast<int>((212u * 1024u) / row_bytes);
+  // same choice of family as the single-vector dispatch
+  const bool want_row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
+  const bool row = want_row && row_kernel_fits(h, elem) && fit >= 2;
+  if (row) {
+    const int group = fit < 4 ? fit : 4;
+    for (int v0 = 0; v0 < nv; v0 += group) {
+      const int k = nv - v0 < group ? nv - v0 : group;
+      const void *xv = xc + v0 * ldx * elem;
+      void *yv = yc + v0 * ldy * elem;
+      const int r = k == 1 ? launch_sigma(h, xv, yv, precision, st)
+                    : precision == DOCI_FP64 ? launch_row_multi<double>(h, xv, ldx, yv, ldy, k, st)
+                                             : launch_row_multi<float>(h, xv, ldx, yv, ldy, k, st);
+      if (r != DOCI_OK) return r;
+    }
+    return DOCI_OK;
+  }
+  if (!want_row || !row_kernel_fits(h, elem))
+    return precision == DOCI_FP64 ? launch_gather_multi_typed<double>(h, x, ldx, y, ldy, nv, st)
+                                  : launch_gather_multi_typed<float>(h, x, ldx, y, ldy, nv, st);
+  // otherwise one vector at a time
+  for (int v = 0; v < nv; ++v) {
+    const int r = launch_sigma(h, xc + v * ldx * elem, yc + v * ldy * elem, precision, st);
+    if (r) return r;
+  }
+  return DOCI_OK;
 }
 
 int launch_diagonal(doci_ham *h, cudaStream_t st) {

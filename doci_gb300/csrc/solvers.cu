@@ -85,6 +85,34 @@ int MatvecOp::apply(const void *d_x, void *d_y, int precision, cudaStream_t st) 
   return DOCI_OK;
 }
 
+int MatvecOp::apply_multi(const void *d_x, size_t ldx, void *d_y, size_t ldy, int nv, int precision,
+                          cudaStream_t st) {
+  const size_t es = precision == DOCI_FP64 ? 8 : 4;
+  if (!ham) {
+    for (int v = 0; v < nv; ++v) {
+      const int s = apply(static_cast<const char *>(d_x) + v * ldx * es, static_cast<char *>(d_y) + v * ldy * es,
+                          precision, st);
+      if (s != DOCI_OK) return s;
+    }
+    return DOCI_OK;
+  }
+  if (events_on) cudaEventRecord(ev0, st);
+  int s = DOCI_OK;
+  for (int v0 = 0; v0 < nv && s == DOCI_OK; v0 += 4) {
+    const int k = nv - v0 < 4 ? nv - v0 : 4;
+    s = launch_sigma_multi(ham, static_cast<const char *>(d_x) + v0 * ldx * es, ldx,
+                           static_cast<char *>(d_y) + v0 * ldy * es, ldy, k, precision, st);
+  }
+  if (events_on) {
+    cudaEventRecord(ev1, st);
+    cudaEventSynchronize(ev1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    sigma_seconds += ms * 1e-3;
+  }
+  return s;
+}
+
 void MatvecOp::enable_timing() {
   if (!events_on && ham) {
     cudaEventCreate(&ev0);
@@ -238,7 +266,8 @@ template int davidson_run<float>(MatvecOp &, size_t, const double *, float *, co
 // Block Davidson (nroots lowest eigenpairs).  Each iteration appends the
 // preconditioned residuals of the unconverged roots, each orthogonalised by
 // classical Gram-Schmidt twice against the whole basis (skipped if it has no
-// component left), computes their sigmas and the new subspace columns, and
+// component left), computes their sigmas in one multi-vector pass and the new
+// subspace columns, and
 // re-diagonalises; the basis restarts from the `keep` lowest Ritz vectors
 // when the next block would not fit.
 // ---------------------------------------------------------------------------
@@ -265,10 +294,10 @@ int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, con
     DOCI_CUDA(cudaStreamSynchronize(st));
     return DOCI_OK;
   };
-  // append the vector in `t` (orthonormalised against V_0..V_{m-1}); returns
-  // false when nothing independent is left
+  // orthonormalise the vector in `t` against V_0..V_{m-1} into V_m (no
+  // sigma yet); `added` is false when nothing independent is left
   int m = 0;
-  auto append = [&](S *t, bool *added) -> int {
+  auto orth = [&](S *t, bool *added) -> int {
     *added = false;
     double n0;
     DOCI_TRY(vec_multidot<S>(t, D, 1, t, D, dp, st));
@@ -291,13 +320,22 @@ int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, con
     const double n1 = red[0];
     if (!(n1 > 1e-20 * n0) || !(n1 > 0)) return DOCI_OK;  // no independent direction left
     DOCI_TRY(vec_gs_finish<S>(Vp, D, 0, nullptr, 1.0 / std::sqrt(n1), D, t, Vp + static_cast<size_t>(m) * D, dp, st));
-    DOCI_TRY(op.apply(Vp + static_cast<size_t>(m) * D, VAp + static_cast<size_t>(m) * D, precision, st));
-    out->sigmas++;
-    DOCI_TRY(vec_multidot<S>(Vp, D, m + 1, VAp + static_cast<size_t>(m) * D, D, dp, st));
-    DOCI_TRY(fetch(m + 1));
-    for (int i = 0; i <= m; ++i) Sm[m * maxv + i] = red[i];
     ++m;
     *added = true;
+    return DOCI_OK;
+  };
+  // sigmas of the new basis vectors V_m0..V_{m-1} in one multi-vector pass,
+  // then their subspace columns
+  auto extend = [&](int m0) -> int {
+    if (m == m0) return DOCI_OK;
+    DOCI_TRY(op.apply_multi(Vp + static_cast<size_t>(m0) * D, D, VAp + static_cast<size_t>(m0) * D, D, m - m0,
+                            precision, st));
+    out->sigmas += m - m0;
+    for (int i = m0; i < m; ++i) {
+      DOCI_TRY(vec_multidot<S>(Vp, D, i + 1, VAp + static_cast<size_t>(i) * D, D, dp, st));
+      DOCI_TRY(fetch(i + 1));
+      for (int k = 0; k <= i; ++k) Sm[i * maxv + k] = red[k];
+    }
     return DOCI_OK;
   };
 
@@ -308,9 +346,10 @@ int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, con
   // start block
   for (int r = 0; r < R; ++r) {
     bool added;
-    DOCI_TRY(append(d_T + static_cast<size_t>(r) * D, &added));
+    DOCI_TRY(orth(d_T + static_cast<size_t>(r) * D, &added));
   }
   if (m == 0) return DOCI_ERR_INVALID;
+  DOCI_TRY(extend(0));
   while (true) {
     ++its;
     jacobi_eig(m, Sm.data(), maxv, w.data(), Y.data());
@@ -352,13 +391,13 @@ int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, con
         break;
       }
     }
-    int added_any = 0;
+    const int m0 = m;
     for (int q = 0; q < nnew; ++q) {
       bool added;
-      DOCI_TRY(append(Tp + static_cast<size_t>(q) * D, &added));
-      added_any += added;
+      DOCI_TRY(orth(Tp + static_cast<size_t>(q) * D, &added));
     }
-    if (!added_any) break;
+    if (m == m0) break;
+    DOCI_TRY(extend(m0));
   }
   const int nr = R < m ? R : m;
   for (int r = 0; r < nr; ++r) {

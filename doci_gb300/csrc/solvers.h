@@ -22,6 +22,9 @@ struct MatvecOp {
   bool events_on = false;
   cudaEvent_t ev0{}, ev1{};
   int apply(const void *d_x, void *d_y, int precision, cudaStream_t st);
+  // nv vectors x + v ldx -> y + v ldy (consecutive columns); the device sigma
+  // shares its neighbour work over up to four vectors per launch
+  int apply_multi(const void *d_x, size_t ldx, void *d_y, size_t ldy, int nv, int precision, cudaStream_t st);
   void enable_timing();
   ~MatvecOp();
 };

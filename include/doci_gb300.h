@@ -140,13 +140,28 @@ const double *doci_ham_diagonal_device(const doci_ham *ham);
  * stream (NULL = the default stream). */
 int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *stream);
 
+/* Block sigma Y_v = H X_v for v < nv on device buffers: X and Y column-major
+ * with leading dimensions ldx, ldy >= D (elements).  The neighbour ranks and
+ * hop weights of each determinant are computed once per launch for up to
+ * four vectors (larger nv runs in groups of four), so a block of vectors
+ * costs much less than nv doci_sigma calls.  Results agree with doci_sigma to
+ * rounding (identical when both use the same kernel).  No counterpart in the
+ * reference, whose matvec (doci.c:164-238) takes one vector; used by the
+ * block Davidson of doci_solve_roots.  Asynchronous on stream (NULL = the
+ * default stream). */
+int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int64_t ldy, int nv, int precision,
+                     void *stream);
+
 /* Sigma kernel selection for a handle: 0 automatic (default: with a row
  * tiling, kind 3 for FP32 and kind 4 for FP64, the fastest measured; else
  * kind 1), 1 the per-determinant gather kernel, 2 the row pass plus a
  * column-panel pass for the row-part hops, 3 the row pass alone doing all
  * hops, 4 the phase-ordered row pass (cross hops staged one source row at a
- * time), 5 kind 4 plus the column-panel pass.  2-5 fall back to 1 when the
- * handle has no row tiling.  For tests and tuning. */
+ * time), 5 kind 4 plus the column-panel pass, 6 the (N-1)-pair form (FP32
+ * only: gather the L neighbours of every (N-1)-pair set, multiply by K on the
+ * tensor cores, scatter-add; atomic adds, so the last bits vary between
+ * runs; FP64 requests use the automatic choice).  2-6 fall back to 1 when
+ * the handle has no row tiling.  For tests and tuning. */
 int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
 
 /* Same on host buffers; copies in and out inside the call, synchronous. */

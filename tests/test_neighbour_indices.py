@@ -11,6 +11,7 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "host_checks", "neighbours_check.cu")
 ROW_SRC = os.path.join(HERE, "host_checks", "row_check.cu")
+PAIR_SRC = os.path.join(HERE, "host_checks", "pair_check.cu")
 
 
 @pytest.fixture(scope="module")
@@ -55,5 +56,29 @@ def row_exe(tmp_path_factory):
 ])
 def test_row_kernel_ranks(row_exe, L, N, split, rs, cs):
     r = subprocess.run([row_exe, str(L), str(N), str(split), str(rs), str(cs)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad=0" in r.stdout
+
+
+@pytest.fixture(scope="module")
+def pair_exe(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    out = str(tmp_path_factory.mktemp("pairc") / "pair_check")
+    subprocess.run([nvcc, "-O2", "-std=c++17", "-diag-suppress=20011", PAIR_SRC, "-o", out], check=True)
+    return out
+
+
+@pytest.mark.parametrize("L,N,split,bs,ss", [
+    # whole spaces: every determinant reached once per pair it holds
+    (10, 5, 6, 1, 1), (12, 6, 8, 1, 1), (12, 3, 8, 1, 1), (12, 11, 8, 1, 1), (14, 7, 9, 1, 1),
+    (16, 8, 10, 1, 1), (18, 9, 9, 1, 1), (20, 10, 9, 1, 1), (9, 0, 8, 1, 1), (9, 9, 8, 1, 1),
+    (17, 1, 16, 1, 1), (17, 16, 16, 1, 1), (32, 2, 8, 1, 1), (22, 11, 11, 1, 1),
+    # sampled large spaces: every visited index in range and equal to the direct rank
+    (32, 16, 16, 37, 101), (28, 14, 16, 11, 31), (32, 30, 8, 3, 1), (26, 4, 12, 1, 1), (24, 12, 13, 7, 11),
+])
+def test_pair_form_ranks(pair_exe, L, N, split, bs, ss):
+    r = subprocess.run([pair_exe, str(L), str(N), str(split), str(bs), str(ss)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad=0" in r.stdout

@@ -50,7 +50,7 @@ def test_golden_sigma_diag_bits(name, fcidump, dg):
         assert np.array_equal(ranks.cpu().numpy(), np.arange(h.D))
 
 
-@pytest.mark.parametrize("kernel", ["gather", "row", "row1", "rowx", "rowxc"])
+@pytest.mark.parametrize("kernel", ["gather", "row", "row1", "rowx", "rowxc", "pair"])
 @pytest.mark.parametrize("L,N,seed", [(16, 8, 21), (18, 5, 22), (20, 10, 23), (12, 1, 24), (12, 11, 25),
                                       (7, 0, 26), (6, 6, 27), (32, 2, 28), (32, 30, 29), (24, 12, 30),
                                       (22, 11, 31), (26, 4, 32)])
@@ -91,7 +91,7 @@ def test_addressing_full_size_properties(synth, dg):
             assert all(bin(int(v)).count("1") == 16 for v in b[:64])
 
 
-@pytest.mark.parametrize("kernel", ["gather", "row", "row1", "rowx", "rowxc"])
+@pytest.mark.parametrize("kernel", ["gather", "row", "row1", "rowx", "rowxc", "pair"])
 def test_sigma_full_size_symmetry_and_linearity(kernel, synth, dg):
     """L=28, N=14 (D = 40,116,600): H is symmetric, sigma is linear, and
     sampled rows agree with the oracle's gather form."""
@@ -126,7 +126,7 @@ def test_sigma_full_size_symmetry_and_linearity(kernel, synth, dg):
         assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("kernel", ["gather", "row", "row1", "rowx", "rowxc"])
+@pytest.mark.parametrize("kernel", ["gather", "row", "row1", "rowx", "rowxc", "pair"])
 def test_sigma_L32_fp32_vs_oracle_samples(kernel, synth, dg):
     """L=32, N=16 (D = 601,080,390), FP32: sampled rank windows across the
     whole space (start, middle, end) against the FP64 oracle gather form."""
@@ -169,3 +169,41 @@ def test_default_stream_orders_after_caller_work(synth, dg):
             outs.append(y)
         torch.cuda.synchronize()
         assert (outs[0] - outs[1]).abs().max().item() <= 2e-6 * outs[0].abs().max().item()
+
+
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row1"])
+@pytest.mark.parametrize("L,N,seed,nv", [(16, 8, 41, 3), (20, 10, 42, 4), (12, 1, 43, 2), (24, 12, 44, 7),
+                                         (18, 17, 45, 4), (26, 4, 46, 5)])
+def test_sigma_block_vs_oracle(L, N, seed, nv, kernel, synth, dg):
+    """doci_sigma_block: nv column-major vectors with padded leading
+    dimensions against the oracle's matvec of each column (FP64 1e-12, FP32
+    2e-6 of max|y|), and against doci_sigma column by column."""
+    torch = torch_cuda()
+    p = synth(L, N, seed)
+    o = oracle.Ham(p)
+    with dg.Hamiltonian.from_fcidump(p) as h:
+        h.set_sigma_kernel(kernel)
+        D = h.D
+        ldx, ldy = D + 5, D + 3
+        rng = np.random.default_rng(seed)
+        X = rng.standard_normal((nv, D))
+        refs = [o.matvec(X[v]) for v in range(nv)]
+        for prec, dt, tol in ((dg.FP64, torch.float64, TOL64), (dg.FP32, torch.float32, TOL32)):
+            xb = torch.zeros(nv * ldx, dtype=dt, device="cuda")
+            for v in range(nv):
+                xb[v * ldx:v * ldx + D] = torch.from_numpy(X[v]).to(dt)
+            yb = torch.full((nv * ldy,), 7.0, dtype=dt, device="cuda")
+            h.sigma_block_device(xb.data_ptr(), ldx, yb.data_ptr(), ldy, nv, prec)
+            y1 = torch.empty(D, dtype=dt, device="cuda")
+            torch.cuda.synchronize()
+            for v in range(nv):
+                y = yb[v * ldy:v * ldy + D].double().cpu().numpy()
+                assert np.abs(y - refs[v]).max() <= tol * np.abs(refs[v]).max()
+                if v < nv - 1:  # padding between columns untouched
+                    assert bool((yb[v * ldy + D:(v + 1) * ldy] == 7.0).all())
+                h.sigma_device(xb[v * ldx:].data_ptr(), y1.data_ptr(), prec)
+                torch.cuda.synchronize()
+                ys = y1.double().cpu().numpy()
+                assert np.abs(y - ys).max() <= tol * np.abs(refs[v]).max()
+                if kernel != "auto" or prec == dg.FP32:  # same kernel family: same summation order
+                    assert np.array_equal(y, ys)
