@@ -244,38 +244,5 @@ inline void build_cross_tables(int sp, const uint32_t *B, int BCstride, std::vec
   }
 }
 
-// Neighbours of an (N-1)-pair set S = (R', C') of the pair-form sigma
-// (sigma_pair.cu): S has colex rank sidx among the jp-subsets C' (bit mask Cm)
-// of the sp column orbitals.  For every orbital o < L not in S,
-// visit(o, kind, where) gets the determinant S u o:
-//   kind 0: column orbital, where = colex(C' u o) in row R' (the row's
-//           position n_own - 1 - where);
-//   kind 1: row orbital, where = sup[o - sp] - sidx, a global rank (sup[b] is
-//           the start of row R' u b plus C(sp, jp) - 1, or ~0 when b is in R').
-// Orbitals are walked from the top so that the colex suffix sums
-// sum_{t >= p} C(c_t, t + 2) - C(c_t, t + 1) build up on the way.
-template <int BC, typename F>
-DOCI_HD void pair_neighbours(uint32_t sidx, uint32_t Cm, int jp, int sp, int L, const uint32_t *B,
-                             const uint32_t *sup, F &&visit) {
-  int cnt = 0;          // elements of C' above o
-  uint32_t suffix = 0;
-#pragma unroll
-  for (int o = 31; o >= 0; --o) {
-    if (o < sp) {
-      if ((Cm >> o) & 1u) {
-        const int t = jp - 1 - cnt;
-        suffix += B[o * BC + t + 2] - B[o * BC + t + 1];
-        ++cnt;
-      } else {
-        const int p = jp - cnt;  // elements of C' below o
-        visit(o, 0, sidx + B[o * BC + p + 1] + suffix);
-      }
-    } else if (o < L) {
-      const uint32_t base = sup[o - sp];
-      if (base != 0xffffffffu) visit(o, 1, base - sidx);
-    }
-  }
-}
-
 }  // namespace dev
 }  // namespace doci

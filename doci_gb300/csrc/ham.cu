@@ -70,7 +70,8 @@ void ham_release(doci_ham *h) {
   h->d_rows = h->d_rowstart = h->d_sector_rs = nullptr;
   h->d_sector_off = nullptr;
   h->d_panels[0] = h->d_panels[1] = nullptr;
-  h->d_pblocks = h->d_kfrag = nullptr;
+  h->d_pblocks = nullptr;
+  h->d_kfrag = nullptr;
   h->npblocks = 0;
   h->d_rem = h->d_ins = h->d_tab_off = nullptr;
   h->h_diag = nullptr;

@@ -97,10 +97,10 @@ struct doci_ham {
   uint32_t *d_rem = nullptr, *d_ins = nullptr, *d_tab_off = nullptr;
   // pair form (sigma_pair.cu): one block per (N-1)-pair set's row part R',
   // {own row start or ~0, mask | k' << 24}, largest first; the K matrix split
-  // into TF32 high and low parts in mma fragment order
+  // into TF32 high and low parts (2 x 32 x 32 floats)
   uint32_t *d_pblocks = nullptr;
   int npblocks = 0;
-  uint32_t *d_kfrag = nullptr;
+  void *d_kfrag = nullptr;
 
   // host diagonal for doci_get_diagonal (lazy)
   double *h_diag = nullptr;

@@ -34,8 +34,10 @@ namespace {
 
 constexpr int kPairThreads = 256;
 constexpr int kPairWarps = kPairThreads / 32;
-constexpr int kTileStride = 36;  // floats per tile row: conflict-free fragment loads and float4 row access
 constexpr uint32_t kNone = 0xffffffffu;
+// tile[q][s] (orbital-major): mma fragment loads (bank 8t + g) and the
+// same-orbital writes of a warp's 32 sets are free of bank conflicts
+constexpr int kTileStride = 40;
 
 struct PairShape {
   uint32_t D;
@@ -43,10 +45,10 @@ struct PairShape {
 };
 
 struct PairSmem {
-  uint32_t binom[kBinomRows * kBinomCols];
-  uint4 kfrag[4 * 4 * 32];                   // [k step][n tile][lane]: {b0 hi, b1 hi, b0 lo, b1 lo}
-  float tile[kPairWarps][32][kTileStride];   // per warp: X rows, then Y rows, one per thread
-  uint32_t sup[32];                          // row bit b: start of row R' u b plus n_s - 1, or kNone
+  uint4 kfrag[4 * 4 * 32];                   // this block's K, [k step][n tile][lane]: {b0 hi, b1 hi, b0 lo, b1 lo}
+  float tile[kPairWarps][32][kTileStride];   // per warp: X_S then Y_S, column s = the warp's 32 sets
+  uint32_t hole_rs[32];                      // row-part holes b of R': start of row R' u b
+  int hole_o[32];                            // and their mirrored orbitals split + b
 };
 
 __device__ __forceinline__ uint32_t to_tf32(float f) {
@@ -64,21 +66,29 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+__device__ __forceinline__ uint32_t lane_of(const uint4 &v, int i) {
+  return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
 __global__ void pair_init_kernel(uint32_t D, const float *__restrict__ diag, const float *__restrict__ x,
                                  float *__restrict__ y) {
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < D; t += gridDim.x * blockDim.x)
     y[t] = diag[t] * x[t];
 }
 
+// One block of sets S = (R', C') per iteration: C' runs over the jp-subsets
+// of the column orbitals (column position c in a row of C(split, jp)
+// columns).  The MMA's orbital axis is compacted to the column orbitals
+// followed by the row-part holes of R' (the row-part elements of R' are in
+// every S, so their X entries are zero).
 __global__ void __launch_bounds__(kPairThreads, 2)
 sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t *__restrict__ rowstart_of,
-                  const uint32_t *__restrict__ g_binom, const uint4 *__restrict__ g_kfrag,
+                  const uint32_t *__restrict__ g_binom, const float *__restrict__ g_ksplit,
+                  const uint32_t *__restrict__ ins, const uint32_t *__restrict__ ins_off,
                   const float *__restrict__ x, float *__restrict__ y) {
   __shared__ __align__(16) PairSmem sm;
   extern __shared__ __align__(16) float acc[];  // own row: hop sums into row R'
-  for (int t = threadIdx.x; t < kBinomRows * kBinomCols; t += blockDim.x) sm.binom[t] = g_binom[t];
-  for (int t = threadIdx.x; t < 4 * 4 * 32; t += blockDim.x) sm.kfrag[t] = g_kfrag[t];
-  const uint32_t *B = sm.binom;
+  const uint32_t *B = g_binom;
   const int sp = s.split;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, tq = lane & 3;
@@ -88,99 +98,122 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
     const uint2 bw = blocks[blk];
     const uint32_t own = bw.x, mask = bw.y & 0xffffffu;
     const int kp = static_cast<int>(bw.y >> 24), jp = s.N - 1 - kp;
-    __syncthreads();  // previous block's flush is done with acc and sup
-    const uint32_t n_s = B[sp * kBinomCols + jp];
-    const uint32_t n_own = jp + 1 <= sp ? B[sp * kBinomCols + jp + 1] : 0u;
-    if (threadIdx.x < 32) {
-      const int b = threadIdx.x;
-      uint32_t v = kNone;
-      if (b < s.na && !((mask >> b) & 1u)) v = rowstart_of[mask | (1u << b)] + n_s - 1u;
-      sm.sup[b] = v;
+    const int nhr = s.na - kp, keff = sp + nhr, nk = (keff + 7) >> 3, nch = sp - jp;
+    __syncthreads();  // previous block's flush is done with acc, holes and fragments
+    const uint32_t n_s = __ldg(B + sp * kBinomCols + jp);
+    const uint32_t n_own = jp + 1 <= sp ? __ldg(B + sp * kBinomCols + jp + 1) : 0u;
+    if (warp == 0) {
+      const bool hole = lane < s.na && !((mask >> lane) & 1u);
+      const uint32_t hb = __ballot_sync(0xffffffffu, hole);
+      if (hole) {
+        const int h = __popc(hb & ((1u << lane) - 1u));
+        sm.hole_rs[h] = rowstart_of[mask | (1u << lane)];
+        sm.hole_o[h] = sp + lane;
+      }
     }
     for (uint32_t c = threadIdx.x; c < n_own; c += blockDim.x) acc[c] = 0.f;
     __syncthreads();
-    const uint32_t own_last = own + n_own - 1u;
+    for (int e = threadIdx.x; e < 4 * 4 * 32; e += blockDim.x) {
+      const int kt = e >> 7, nt = (e >> 5) & 3, ln = e & 31;
+      const int a0 = 8 * kt + (ln & 3), a1 = a0 + 4, i = 8 * nt + (ln >> 2);
+      auto orb = [&](int col) { return col < sp ? col : col < keff ? sm.hole_o[col - sp] : -1; };
+      const int o0 = orb(a0), o1 = orb(a1), oi = orb(i);
+      const bool v0 = o0 >= 0 && oi >= 0, v1 = o1 >= 0 && oi >= 0;
+      const float *khi = g_ksplit, *klo = g_ksplit + 32 * 32;
+      sm.kfrag[e] = make_uint4(v0 ? __float_as_uint(__ldg(khi + o0 * 32 + oi)) : 0u,
+                               v1 ? __float_as_uint(__ldg(khi + o1 * 32 + oi)) : 0u,
+                               v0 ? __float_as_uint(__ldg(klo + o0 * 32 + oi)) : 0u,
+                               v1 ? __float_as_uint(__ldg(klo + o1 * 32 + oi)) : 0u);
+    }
+    __syncthreads();
+    const uint32_t *ins_blk = ins + ins_off[jp];
 
     for (uint32_t s0 = 0; s0 < n_s; s0 += kPairThreads) {
-      if (s0 + 32u * warp >= n_s) break;  // this warp's rows are all past the block (warp-uniform)
-      const uint32_t sidx = s0 + threadIdx.x;
-      const bool live = sidx < n_s;
-      const uint32_t Cm = live ? dev::colex_unrank<kBinomCols>(sidx, sp, jp, B) : 0u;
-      // gather X_S into this thread's tile row
+      if (s0 + 32u * warp >= n_s) break;  // this warp's sets are all past the block (warp-uniform)
+      const uint32_t c = s0 + threadIdx.x;
+      const bool live = c < n_s;
       {
-        float xv[32];
+        float4 *tz = reinterpret_cast<float4 *>(&tile[0][0]);
 #pragma unroll
-        for (int o = 0; o < 32; ++o) xv[o] = 0.f;
-        if (live)
-          dev::pair_neighbours<kBinomCols>(sidx, Cm, jp, sp, s.L, B, sm.sup, [&](int o, int kind, uint32_t where) {
-            xv[o] = __ldg(x + (kind == 0 ? own_last - where : where));
-          });
+        for (int z = lane; z < 32 * kTileStride / 4; z += 32) tz[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      __syncwarp();
+      // gather X_S: column holes of C' (row R', positions from the insertion
+      // table) and the row-part holes of R' (rows R' u b, column c)
+      uint4 ent[4];
+      if (live) {
+        const uint4 *ip = reinterpret_cast<const uint4 *>(ins_blk + 16u * c);
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-          *reinterpret_cast<float4 *>(&tile[lane][4 * q]) = make_float4(xv[4 * q], xv[4 * q + 1], xv[4 * q + 2], xv[4 * q + 3]);
+        for (int u = 0; u < 4; ++u)
+          if (4 * u < nch) ent[u] = __ldg(ip + u);
+#pragma unroll
+        for (int h = 0; h < 16; ++h)
+          if (h < nch) {
+            const uint32_t e = lane_of(ent[h >> 2], h & 3);
+            tile[e & 0xffu][lane] = __ldg(x + own + (e >> 8));
+          }
+        for (int h = 0; h < nhr; ++h) tile[sp + h][lane] = __ldg(x + sm.hole_rs[h] + c);
       }
       __syncwarp();
       // Y = X K on the tensor cores: 3xTF32 (lo*hi + hi*lo + hi*hi)
-      float c[2][4][4];
+      float cc[2][4][4];
 #pragma unroll
       for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
-          for (int e = 0; e < 4; ++e) c[mt][nt][e] = 0.f;
+          for (int e = 0; e < 4; ++e) cc[mt][nt][e] = 0.f;
 #pragma unroll
       for (int kt = 0; kt < 4; ++kt) {
-        uint32_t ah[2][4], al[2][4];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-          const int r0 = 16 * mt + g, c0 = 8 * kt + tq;
-          const float f[4] = {tile[r0][c0], tile[r0 + 8][c0], tile[r0][c0 + 4], tile[r0 + 8][c0 + 4]};
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            ah[mt][e] = to_tf32(f[e]);
-            al[mt][e] = to_tf32(f[e] - __uint_as_float(ah[mt][e]));
-          }
-        }
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-          const uint4 b = sm.kfrag[(kt * 4 + nt) * 32 + lane];
+        if (kt < nk) {
+          uint32_t ah[2][4], al[2][4];
 #pragma unroll
           for (int mt = 0; mt < 2; ++mt) {
-            mma_tf32(c[mt][nt], al[mt], b.x, b.y);
-            mma_tf32(c[mt][nt], ah[mt], b.z, b.w);
-            mma_tf32(c[mt][nt], ah[mt], b.x, b.y);
+            const int r0 = 16 * mt + g, k0 = 8 * kt + tq;
+            const float f[4] = {tile[k0][r0], tile[k0][r0 + 8], tile[k0 + 4][r0], tile[k0 + 4][r0 + 8]};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              ah[mt][e] = to_tf32(f[e]);
+              al[mt][e] = to_tf32(f[e] - __uint_as_float(ah[mt][e]));
+            }
           }
+#pragma unroll
+          for (int nt = 0; nt < 4; ++nt)
+            if (nt < nk) {
+              const uint4 b = sm.kfrag[(kt * 4 + nt) * 32 + lane];
+#pragma unroll
+              for (int mt = 0; mt < 2; ++mt) {
+                mma_tf32(cc[mt][nt], al[mt], b.x, b.y);
+                mma_tf32(cc[mt][nt], ah[mt], b.z, b.w);
+                mma_tf32(cc[mt][nt], ah[mt], b.x, b.y);
+              }
+            }
         }
       }
       __syncwarp();
 #pragma unroll
       for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-          const int r0 = 16 * mt + g, c0 = 8 * nt + 2 * tq;
-          *reinterpret_cast<float2 *>(&tile[r0][c0]) = make_float2(c[mt][nt][0], c[mt][nt][1]);
-          *reinterpret_cast<float2 *>(&tile[r0 + 8][c0]) = make_float2(c[mt][nt][2], c[mt][nt][3]);
-        }
+        for (int nt = 0; nt < 4; ++nt)
+          if (nt < nk) {
+            const int r0 = 16 * mt + g, q0 = 8 * nt + 2 * tq;
+            tile[q0][r0] = cc[mt][nt][0];
+            tile[q0 + 1][r0] = cc[mt][nt][1];
+            tile[q0][r0 + 8] = cc[mt][nt][2];
+            tile[q0 + 1][r0 + 8] = cc[mt][nt][3];
+          }
       __syncwarp();
       // scatter Y_S back to the same determinants
       if (live) {
-        float yv[32];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const float4 v = *reinterpret_cast<const float4 *>(&tile[lane][4 * q]);
-          yv[4 * q] = v.x;
-          yv[4 * q + 1] = v.y;
-          yv[4 * q + 2] = v.z;
-          yv[4 * q + 3] = v.w;
-        }
-        dev::pair_neighbours<kBinomCols>(sidx, Cm, jp, sp, s.L, B, sm.sup, [&](int o, int kind, uint32_t where) {
-          if (kind == 0)
-            atomicAdd(&acc[n_own - 1u - where], yv[o]);
-          else
-            atomicAdd(y + where, yv[o]);
-        });
+        for (int h = 0; h < 16; ++h)
+          if (h < nch) {
+            const uint32_t e = lane_of(ent[h >> 2], h & 3);
+            atomicAdd(&acc[e >> 8], tile[e & 0xffu][lane]);
+          }
+        for (int h = 0; h < nhr; ++h) atomicAdd(y + sm.hole_rs[h] + c, tile[sp + h][lane]);
       }
-      __syncwarp();  // the tile is rewritten by the next round's gather
+      __syncwarp();  // the tile is cleared by the next round
     }
     __syncthreads();
     for (uint32_t c = threadIdx.x; c < n_own; c += blockDim.x) atomicAdd(y + own + c, acc[c]);
@@ -200,32 +233,24 @@ float round_tf32(double v) {
 }  // namespace
 
 bool pair_fits(const doci_ham *h) {
-  if (h->split < 1 || h->nrows < 1 || !h->d_pblocks || h->npblocks < 1) return false;
+  if (h->split < 1 || h->split > 16 || h->nrows < 1 || !h->d_pblocks || h->npblocks < 1) return false;
+  if (!h->d_ins || !h->d_tab_off) return false;
   if (h->L - h->split > 24) return false;
   return static_cast<size_t>(h->max_row) * sizeof(float) <= 100 * 1024;
 }
 
 int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
   const int L = h->L, N = h->N, sp = h->split, na = L - sp;
-  // K in mma B-fragment order, split into TF32 high and low parts (from FP64)
-  std::vector<uint32_t> kf(4 * 4 * 32 * 4);
-  for (int kt = 0; kt < 4; ++kt)
-    for (int nt = 0; nt < 4; ++nt)
-      for (int lane = 0; lane < 32; ++lane) {
-        const int gg = lane >> 2, t = lane & 3, i = 8 * nt + gg;
-        const int a0 = 8 * kt + t, a1 = a0 + 4;
-        auto K = [&](int a, int b) -> double {
-          return a < L && b < L ? h->Kp[(L - 1 - a) * L + (L - 1 - b)] : 0.0;
-        };
-        const double k0 = K(a0, i), k1 = K(a1, i);
-        const float h0 = round_tf32(k0), h1 = round_tf32(k1);
-        const float l0 = round_tf32(k0 - h0), l1 = round_tf32(k1 - h1);
-        uint32_t *e = &kf[((kt * 4 + nt) * 32 + lane) * 4];
-        std::memcpy(e + 0, &h0, 4);
-        std::memcpy(e + 1, &h1, 4);
-        std::memcpy(e + 2, &l0, 4);
-        std::memcpy(e + 3, &l1, 4);
-      }
+  // K (mirrored orbitals, zero outside 0..L-1) split into TF32 high and low
+  // parts from the FP64 values: [hi 32 x 32 | lo 32 x 32]
+  std::vector<float> ks(2 * 32 * 32, 0.f);
+  for (int a = 0; a < L; ++a)
+    for (int b = 0; b < L; ++b) {
+      const double k = h->Kp[(L - 1 - a) * L + (L - 1 - b)];
+      const float hi = round_tf32(k);
+      ks[a * 32 + b] = hi;
+      ks[32 * 32 + a * 32 + b] = round_tf32(k - hi);
+    }
   // one block per row part R' of an (N-1)-set, largest first
   std::vector<std::pair<uint64_t, std::pair<uint32_t, uint32_t>>> bl;
   for (uint32_t mask = 0; mask < (1u << na); ++mask) {
@@ -242,8 +267,8 @@ int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
     flat.push_back(e.second.second);
   }
   h->npblocks = static_cast<int>(bl.size());
-  DOCI_CUDA(cudaMallocAsync(&h->d_kfrag, kf.size() * sizeof(uint32_t), h->stream));
-  DOCI_CUDA(cudaMemcpyAsync(h->d_kfrag, kf.data(), kf.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_kfrag, ks.size() * sizeof(float), h->stream));
+  DOCI_CUDA(cudaMemcpyAsync(h->d_kfrag, ks.data(), ks.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   if (!flat.empty()) {
     DOCI_CUDA(cudaMallocAsync(&h->d_pblocks, flat.size() * sizeof(uint32_t), h->stream));
     DOCI_CUDA(cudaMemcpyAsync(h->d_pblocks, flat.data(), flat.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
@@ -272,7 +297,8 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
   if (grid > h->npblocks) grid = h->npblocks;
   sigma_pair_kernel<<<grid, kPairThreads, dyn, st>>>(s, reinterpret_cast<const uint2 *>(h->d_pblocks),
                                                      h->d_rowstart, h->d_binom,
-                                                     reinterpret_cast<const uint4 *>(h->d_kfrag), x, y);
+                                                     reinterpret_cast<const float *>(h->d_kfrag), h->d_ins,
+                                                     h->d_tab_off, x, y);
   DOCI_CUDA(cudaGetLastError());
   return DOCI_OK;
 }

@@ -1,8 +1,11 @@
 // Host-side check of the pair-form sigma's index arithmetic
-// (doci_gb300/csrc/addressing.cuh, dev::pair_neighbours), compiled by nvcc and
-// run on the CPU.  The blocks (row parts R' of the (N-1)-pair sets) are listed
-// by the library's rule; row starts and every neighbour rank are recomputed
-// here from first principles (lexical rank of the neighbour's bitstring).
+// (doci_gb300/csrc/sigma_pair.cu), compiled by nvcc and run on the CPU.  The
+// blocks (row parts R' of the (N-1)-pair sets) are listed by the library's
+// rule and the insertion table is the library's (dev::build_cross_tables);
+// the kernel's formulas are applied to them (column hole h of the set at
+// column c: own row start + (ins >> 8), orbital ins & 255; row-part hole b:
+// start of row R' u b + c), and every neighbour rank is recomputed here from
+// first principles (lexical rank of the neighbour's bitstring).
 // Every set S must visit each orbital outside S exactly once, in range, at the
 // rank of S u o; over a whole space (strides 1) every determinant must be
 // reached exactly N times (once per pair it holds).
@@ -50,6 +53,8 @@ int main(int argc, char **argv) {
     const uint32_t Cb = doci::dev::colex_unrank<BC>(n - 1, sp, j, B.data());
     return direct_rank_mirrored(Cb | (R << sp), L, N);
   };
+  std::vector<uint32_t> rem, ins, off;
+  if (sp <= 16) doci::dev::build_cross_tables(sp, B.data(), BC, rem, ins, off);
   const bool full = bstride == 1 && sstride == 1;
   std::vector<uint8_t> hits(full ? D : 0, 0);
   uint64_t bad = 0, sets = 0, visits = 0;
@@ -61,47 +66,49 @@ int main(int argc, char **argv) {
     const uint32_t n_s = static_cast<uint32_t>(binom(sp, jp));
     const uint32_t n_own = jp + 1 <= sp ? static_cast<uint32_t>(binom(sp, jp + 1)) : 0u;
     const uint64_t own = n_own ? row_start(mask) : ~0ull;
-    uint32_t sup[32];
-    for (int b = 0; b < 32; ++b) {
-      sup[b] = 0xffffffffu;
-      if (b < na && !((mask >> b) & 1u)) sup[b] = static_cast<uint32_t>(row_start(mask | (1u << b)) + n_s - 1);
-    }
-    for (uint32_t sidx = 0; sidx < n_s; sidx += static_cast<uint32_t>(sstride)) {
-      const uint32_t Cm = doci::dev::colex_unrank<BC>(sidx, sp, jp, B.data());
+    // row-part holes in ascending order (the kernel's ballot compaction)
+    std::vector<uint64_t> hole_rs;
+    std::vector<int> hole_o;
+    for (int b = 0; b < na; ++b)
+      if (!((mask >> b) & 1u)) {
+        hole_rs.push_back(row_start(mask | (1u << b)));
+        hole_o.push_back(sp + b);
+      }
+    const int nch = sp - jp, nhr = na - kp;
+    if (static_cast<int>(hole_rs.size()) != nhr || sp + nhr > 32) ++bad;
+    for (uint32_t c = 0; c < n_s; c += static_cast<uint32_t>(sstride)) {
+      // the set S at column c of a row of n_s columns: colex n_s - 1 - c
+      const uint32_t Cm = doci::dev::colex_unrank<BC>(n_s - 1 - c, sp, jp, B.data());
       const uint32_t S = Cm | (mask << sp);
       uint32_t seen = 0;
       ++sets;
-      doci::dev::pair_neighbours<BC>(sidx, Cm, jp, sp, L, B.data(), sup, [&](int o, int kind, uint32_t where) {
+      auto check = [&](int o, uint64_t rank, int tile_q) {
         ++visits;
-        if (o >= L || (S >> o & 1u) || (seen >> o & 1u)) {
+        if (o >= L || (S >> o & 1u) || (seen >> o & 1u) || tile_q < 0 || tile_q >= 32) {
           ++bad;
           return;
         }
         seen |= 1u << o;
-        uint64_t rank;
-        if (kind == 0) {
-          if (o >= sp || where >= n_own) {
-            ++bad;
-            return;
-          }
-          rank = own + (n_own - 1 - where);
-        } else {
-          if (o < sp) {
-            ++bad;
-            return;
-          }
-          rank = where;
-        }
         const uint64_t want = direct_rank_mirrored(S | (1u << o), L, N);
         if (rank != want || rank >= D) {
           if (bad < 5)
-            std::printf("mismatch S=%x o=%d kind=%d rank=%llu want=%llu\n", S, o, kind,
-                        static_cast<unsigned long long>(rank), static_cast<unsigned long long>(want));
+            std::printf("mismatch S=%x o=%d rank=%llu want=%llu\n", S, o, static_cast<unsigned long long>(rank),
+                        static_cast<unsigned long long>(want));
           ++bad;
           return;
         }
         if (full) ++hits[rank];
-      });
+      };
+      for (int h = 0; h < nch; ++h) {
+        const uint32_t e = ins[off[jp] + 16u * c + h];
+        const uint32_t pos = e >> 8, q = e & 0xffu;
+        if (pos >= n_own || q >= static_cast<uint32_t>(sp)) {
+          ++bad;
+          continue;
+        }
+        check(static_cast<int>(q), own + pos, static_cast<int>(q));
+      }
+      for (int h = 0; h < nhr; ++h) check(hole_o[h], hole_rs[h] + c, sp + h);
       const uint32_t outside = doci::dev::low_mask(L) & ~S;
       if (seen != outside) ++bad;
     }
