@@ -109,8 +109,15 @@ int solve_roots(doci_ham *h, const doci_batch_opts &o, cudaStream_t st, doci_roo
     BlockArgs a32 = a;
     a32.tol = o.mixed_tol > o.tol ? o.mixed_tol : o.tol;
     a32.stall_window = 15;
+    // the FP32 phase runs on H - (lowest diagonal element)
+    ShiftedView sv;
+    DOCI_TRY_B(sv.make(h, st));
+    a32.shift = sv.shift;
+    MatvecOp op32;
+    op32.ham = &sv.view;
+    op32.n = D;
     BlockOut o32;
-    DOCI_TRY_B(block_davidson_run<float>(op, D, h->d_diag, static_cast<float *>(T32.p), a32, st, &o32, d_X));
+    DOCI_TRY_B(block_davidson_run<float>(op32, D, h->d_diag, static_cast<float *>(T32.p), a32, st, &o32, d_X));
     its32 = o32.iterations;
     for (int r = 0; r < R; ++r) res->energy_fp32[r] = o32.energy[r];
     DOCI_CUDA(cudaMemcpyAsync(d_T, d_X, sizeof(double) * D * R, cudaMemcpyDeviceToDevice, st));
@@ -141,7 +148,8 @@ int64_t roots_footprint(int L, int N, const doci_batch_opts &o) {
   const int64_t ham = D * 12 + (16ll << 20);  // diagonals, tables
   const int64_t common = D * R * 8 * 2 + D * 8;  // X, T, start-vector scratch
   const int64_t p64 = 2 * mv * D * 8 + R * D * 8;
-  const int64_t p32 = o.mode == DOCI_MODE_MIXED ? 2 * mv * D * 4 + R * D * 4 * 2 : 0;
+  // FP32 phase: basis, start and correction blocks, shifted FP32 diagonal
+  const int64_t p32 = o.mode == DOCI_MODE_MIXED ? 2 * mv * D * 4 + R * D * 4 * 2 + D * 4 : 0;
   return ham + common + std::max(p64, p32) + (4ll << 20);
 }
 

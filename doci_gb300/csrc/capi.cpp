@@ -234,7 +234,7 @@ int doci_multidot(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n
               ? vec_multidot<double>(static_cast<const double *>(d_V), static_cast<size_t>(ld), m,
                                      static_cast<const double *>(d_w), static_cast<size_t>(n), partials, st)
               : vec_multidot<float>(static_cast<const float *>(d_V), static_cast<size_t>(ld), m,
-                                    static_cast<const float *>(d_w), static_cast<size_t>(n), partials, st);
+                                    static_cast<const float *>(d_w), static_cast<size_t>(n), partials, st, true);
   if (s == DOCI_OK) s = vec_reduce(partials, m, d_out, st);
   const cudaError_t e = cudaFreeAsync(partials, st);
   if (s != DOCI_OK) return s;
@@ -272,7 +272,8 @@ int64_t doci_solve_footprint(int L, int n_pairs, const doci_solve_opts *o, int n
   if (o->solver != DOCI_SOLVER_D) {
     solver = D * 8 * 7;  // x, p, Ax, Ap, g, pinv + start
   } else if (o->mode == DOCI_MODE_MIXED) {
-    const int64_t p32 = D * (2 * mv * 4 + 4 + 8), p64 = D * (2 * mv * 8 + 8 + 8);
+    // FP32 phase: basis, start, x, shifted FP32 diagonal
+    const int64_t p32 = D * (2 * mv * 4 + 4 + 8 + 4), p64 = D * (2 * mv * 8 + 8 + 8);
     solver = p32 > p64 ? p32 : p64;
   } else {
     solver = D * (2 * mv * 8 + 8 + 8);
@@ -337,7 +338,17 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
       a32.stall_window = 15;
       a32.print_summary = 0;
       a32.trace_phase = 0;
-      if ((s = davidson_run<float>(op, D, h->d_diag, static_cast<float *>(t32.p), a32, st, &out, d_x))) return s;
+      // the FP32 phase runs on H - (lowest diagonal element)
+      ShiftedView sv;
+      if ((s = sv.make(h, st))) return s;
+      a32.shift = sv.shift;
+      MatvecOp op32;
+      op32.ham = &sv.view;
+      op32.n = D;
+      op32.enable_timing();
+      s = davidson_run<float>(op32, D, h->d_diag, static_cast<float *>(t32.p), a32, st, &out, d_x);
+      op.sigma_seconds += op32.sigma_seconds;
+      if (s) return s;
       res->iterations_fp32 = out.iterations;
       res->energy_fp32 = out.energy;
       its_left -= out.iterations;

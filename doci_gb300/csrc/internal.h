@@ -117,8 +117,11 @@ int ham_build(doci_ham *h, const Integrals &in);
 void ham_release(doci_ham *h);
 int ham_stage(doci_ham *h, size_t bytes);
 // sigma.cu
-int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t s);
-// nv <= 4 vectors x + v ldx -> y + v ldy with the neighbour work shared
+// allow_pair = false keeps the FP32 result run-to-run reproducible (the pair
+// form adds with atomics)
+int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t s, bool allow_pair = true);
+// nv <= 4 vectors x + v ldx -> y + v ldy with the neighbour work shared;
+// never the pair form
 int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv, int precision,
                        cudaStream_t s);
 // resident blocks per SM of a kernel with `dyn` bytes of dynamic shared

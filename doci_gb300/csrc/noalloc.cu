@@ -72,7 +72,7 @@ extern "C" int doci_multidot_noalloc(const void *d_V, int64_t ld, int m, const v
                     ? vec_multidot<double>(static_cast<const double *>(d_V), static_cast<size_t>(ld), m,
                                            static_cast<const double *>(d_w), static_cast<size_t>(n), scratch, st)
                     : vec_multidot<float>(static_cast<const float *>(d_V), static_cast<size_t>(ld), m,
-                                          static_cast<const float *>(d_w), static_cast<size_t>(n), scratch, st);
+                                          static_cast<const float *>(d_w), static_cast<size_t>(n), scratch, st, true);
   if (s != DOCI_OK) return s;
   return vec_reduce(scratch, m, d_out, st);
 }

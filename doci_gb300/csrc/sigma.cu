@@ -881,11 +881,13 @@ unsigned grid_for(uint64_t n) {
 
 }  // namespace
 
-int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t st) {
+int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t st, bool allow_pair) {
   if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
   const size_t elem = precision == DOCI_FP64 ? 8 : 4;
-  // pair form on request (kind 6, FP32 only)
-  if (h->sigma_kernel == 6 && precision == DOCI_FP32 && pair_fits(h))
+  // pair form: on request (kind 6), and the automatic FP32 choice when its
+  // blocks give every SM work (measured fastest there); FP32 only
+  const bool want_pair = h->sigma_kernel == 6 || (h->sigma_kernel == 0 && h->npblocks >= device_sm_count());
+  if (allow_pair && want_pair && precision == DOCI_FP32 && pair_fits(h))
     return launch_pair(h, static_cast<const float *>(x), static_cast<float *>(y), st);
   // row kernel when the row tiling exists, fits, and gives every SM work
   bool row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
@@ -916,7 +918,8 @@ int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, si
   if (nv < 1 || nv > 4 || ldx < h->D || ldy < h->D) return DOCI_ERR_INVALID;
   if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
   const size_t elem = precision == DOCI_FP64 ? 8 : 4;
-  if (nv == 1) return launch_sigma(h, x, y, precision, st);
+  // the block solves stay run-to-run reproducible: no pair form here
+  if (nv == 1) return launch_sigma(h, x, y, precision, st, false);
   const char *xc = static_cast<const char *>(x);
   char *yc = static_cast<char *>(y);
   // row pass: every vector's row staged in shared memory, so the group size
@@ -932,7 +935,7 @@ int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, si
       const int k = nv - v0 < group ? nv - v0 : group;
       const void *xv = xc + v0 * ldx * elem;
       void *yv = yc + v0 * ldy * elem;
-      const int r = k == 1 ? launch_sigma(h, xv, yv, precision, st)
+      const int r = k == 1 ? launch_sigma(h, xv, yv, precision, st, false)
                     : precision == DOCI_FP64 ? launch_row_multi<double>(h, xv, ldx, yv, ldy, k, st)
                                              : launch_row_multi<float>(h, xv, ldx, yv, ldy, k, st);
       if (r != DOCI_OK) return r;
@@ -944,7 +947,7 @@ int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, si
                                   : launch_gather_multi_typed<float>(h, x, ldx, y, ldy, nv, st);
   // otherwise one vector at a time
   for (int v = 0; v < nv; ++v) {
-    const int r = launch_sigma(h, xc + v * ldx * elem, yc + v * ldy * elem, precision, st);
+    const int r = launch_sigma(h, xc + v * ldx * elem, yc + v * ldy * elem, precision, st, false);
     if (r) return r;
   }
   return DOCI_OK;

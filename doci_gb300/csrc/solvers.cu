@@ -61,6 +61,23 @@ double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+int ShiftedView::make(const doci_ham *h, cudaStream_t s) {
+  st = s;
+  view = *h;
+  int64_t idx = 0;
+  DOCI_TRY(vec_argmin(h->d_diag, h->D, &idx, s));
+  DOCI_CUDA(cudaMemcpyAsync(&shift, h->d_diag + idx, sizeof(double), cudaMemcpyDeviceToHost, s));
+  DOCI_CUDA(cudaStreamSynchronize(s));
+  DOCI_CUDA(cudaMallocAsync(&d_diag32, sizeof(float) * h->D, s));
+  DOCI_TRY(vec_shifted_diag32(h->d_diag, shift, d_diag32, h->D, s));
+  view.d_diag32 = d_diag32;
+  return DOCI_OK;
+}
+
+ShiftedView::~ShiftedView() {
+  if (d_diag32) cudaFreeAsync(d_diag32, st);
+}
+
 int MatvecOp::apply(const void *d_x, void *d_y, int precision, cudaStream_t st) {
   if (ham) {
     if (events_on) cudaEventRecord(ev0, st);
@@ -160,6 +177,7 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
   if (a.print_table) std::printf("IT\tINFO\tRESIDUE\tENERGY\n");
   int stall = 0;
   double best = 1e300;
+  double t_norm2 = 0, proj2 = 0;  // ||t||^2 and ||V^T t||^2 from the residual pass
   while (res > a.tol && its++ < a.max_its) {
     // ---- new search vector: orthogonalise t against V, normalise (davidson.c:133-176)
     S *Vm = Vp + static_cast<size_t>(m) * D;
@@ -167,6 +185,12 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
       DOCI_TRY(vec_multidot<S>(d_t, D, 1, d_t, D, dp, st));
       DOCI_TRY(fetch(1));
       DOCI_TRY(vec_gs_finish<S>(Vp, D, 0, nullptr, 1.0 / std::sqrt(red[0]), D, d_t, Vm, dp, st));
+    } else if (sizeof(S) == 4 && t_norm2 - proj2 > 0.5 * t_norm2) {
+      // FP32 basis: t keeps more than half of its norm after one projection,
+      // so one classical Gram-Schmidt pass is enough (the Daniel-Gragg-
+      // Kaufman-Stewart criterion); the residual pass already gave V^T t
+      DOCI_CUDA(cudaMemcpyAsync(d_vec, c.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+      DOCI_TRY(vec_gs_finish<S>(Vp, D, m, d_vec, 1.0 / std::sqrt(t_norm2 - proj2), D, d_t, Vm, dp, st));
     } else {
       DOCI_CUDA(cudaMemcpyAsync(d_vec, c.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
       DOCI_TRY(vec_gs_update<S>(Vp, D, m, d_vec, D, d_t, dp, st));
@@ -203,18 +227,23 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
     // ---- residual, preconditioner, first GS projections (davidson.c:90, :98)
     const double theta = w[0];
     DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
-    DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, theta, d_diag, D, d_t, nullptr, dp, st));
+    DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, theta, d_diag, D, d_t, nullptr, dp, st, a.shift));
     DOCI_TRY(fetch(m + 2));
     res = std::sqrt(red[0]);
-    for (int i = 0; i < m; ++i) c[i] = red[2 + i];
+    t_norm2 = red[1];
+    proj2 = 0;
+    for (int i = 0; i < m; ++i) {
+      c[i] = red[2 + i];
+      proj2 += c[i] * c[i];
+    }
     d_energy = energy - theta;
     energy = theta;
-    if (a.print_table) std::printf("%d\t%d\t%e\t%f\n", its, 0, res, theta);
+    if (a.print_table) std::printf("%d\t%d\t%e\t%f\n", its, 0, res, theta + a.shift);
     if (a.trace && a.trace_count && *a.trace_count < a.trace_len) {
       double *r = a.trace + 4 * (*a.trace_count)++;
       r[0] = a.trace_phase;
       r[1] = res;
-      r[2] = theta;
+      r[2] = theta + a.shift;
       r[3] = now_s() - a.trace_t0;
     }
     // FP32 phase of the mixed mode: stop once the residual has not reached a
@@ -247,7 +276,7 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
     DOCI_TRY(vec_combine<S>(Vp, D, m, d_vec, D, d_x_out, st));
   }
   DOCI_CUDA(cudaStreamSynchronize(st));
-  out->energy = w[0];
+  out->energy = w[0] + a.shift;
   out->residual = res;
   out->iterations = its;
   out->converged = res <= a.tol;
@@ -374,7 +403,7 @@ int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, con
       DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data() + static_cast<size_t>(r) * maxv, sizeof(double) * m,
                                 cudaMemcpyHostToDevice, st));
       S *t = Tp + static_cast<size_t>(nnew) * D;
-      DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, w[r], d_diag, D, t, nullptr, dp, st));
+      DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, w[r], d_diag, D, t, nullptr, dp, st, a.shift));
       DOCI_TRY(fetch(m + 2));  // the residual pass writes m + 2 partials per block
       res[r] = std::sqrt(red[0]);
       worst = res[r] > worst ? res[r] : worst;
@@ -401,7 +430,7 @@ int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, con
   }
   const int nr = R < m ? R : m;
   for (int r = 0; r < nr; ++r) {
-    out->energy[r] = w[r];
+    out->energy[r] = w[r] + a.shift;
     out->residual[r] = res[r];
     if (d_X_out) {
       DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data() + static_cast<size_t>(r) * maxv, sizeof(double) * m,

@@ -34,7 +34,10 @@ struct DavidsonArgs {
   double tol = 1e-8;
   int print_table = 0;    // the -DDAVIDIT table of davidson.c:47-112
   int print_summary = 0;  // "** DAVIDSON ITERATIONS" (davidson.c:114)
-  int stall_window = 0;   // > 0: stop when the residual stops halving (FP32 phase)
+  int stall_window = 0;   // > 0: stop when the residual stops reaching new minima (FP32 phase)
+  // the operator is H - shift (energies are reported + shift; the
+  // preconditioner's diagonal is the unshifted FP64 one)
+  double shift = 0;
   // optional per-iteration records {phase, residual, energy, seconds since
   // trace_t0} (4 doubles each), trace_len records at most
   double *trace = nullptr;
@@ -64,10 +67,28 @@ struct CgOut {
 
 double now_s();  // steady clock, seconds
 
+// The FP32 phase of the mixed mode runs on H - s, s = the lowest diagonal
+// element (the reference determinant's energy): the FP32 rounding of sigma
+// then scales with |H - s| on the determinants that carry the ground state
+// (a few Ha) instead of with |E| (hundreds of Ha at L = 32).  `view` is a copy
+// of the handle whose FP32 diagonal is diag - s (owned here, freed on st).
+struct ShiftedView {
+  doci_ham view;
+  double shift = 0;
+  float *d_diag32 = nullptr;
+  cudaStream_t st = nullptr;
+  int make(const doci_ham *h, cudaStream_t s);
+  ShiftedView() = default;
+  ShiftedView(const ShiftedView &) = delete;
+  ShiftedView &operator=(const ShiftedView &) = delete;
+  ~ShiftedView();
+};
+
 struct BlockArgs {
   int nroots = 1, max_vectors = 16, keep = 0, max_its = 200;
   double tol = 1e-8;         // on every root's residual norm
   int stall_window = 0;      // > 0: stop when the largest residual stops reaching new minima
+  double shift = 0;          // the operator is H - shift, as in DavidsonArgs
 };
 
 struct BlockOut {

@@ -3,7 +3,8 @@
 // The reference runs these steps as BLAS calls on host arrays
 // (davidson.c:133-255, CG.c:74-127).  Here they are fused passes over HBM:
 //  * residual pass: x = V y, r = VA y - theta x, ||r||, the preconditioned
-//    t = r / |diag - theta| (davidson.c:195-227) and the first Gram-Schmidt
+//    t = r / |diag - theta| (davidson.c:195-227; for a shifted operator
+//    H - s the preconditioner uses diag - s - theta) and the first Gram-Schmidt
 //    projections V^T t, all in one read of V and VA;
 //  * Gram-Schmidt: classical GS applied twice (projection pass, update +
 //    second projection pass, final update + normalisation), replacing the
@@ -12,11 +13,15 @@
 //  * deflation V <- V Y[:, :keep] in place (davidson.c:229-255);
 //  * RQ-CG: the 2x2 Gram blocks of CG.c:102-103 in one pass, and the x/Ax/g
 //    updates of CG.c:106-126 in one pass.
-// Storage is double (FP64 mode) or float (FP32 basis of the mixed mode);
-// every product is accumulated in FP64.  Reductions are two-stage
+// Storage is double (FP64 mode) or float (FP32 basis of the mixed mode).
+// FP64 storage: FP64 arithmetic throughout.  FP32 storage: FP32 arithmetic
+// on the shifted operator, FP32 partial sums over short runs added into FP64
+// accumulators (the *_f32 kernels).  Reductions are two-stage
 // (per-block partials, then one block summing them in a fixed order), so
 // results do not depend on timing.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "internal.h"
 #include "vec.h"
@@ -27,7 +32,7 @@ namespace {
 constexpr int kT = 256;
 constexpr int kMaxK = 34;  // outputs of one reduction pass
 
-int grid_blocks() { return device_sm_count() * 2; }
+int grid_blocks() { return device_sm_count() * 4; }
 
 template <int K>
 __device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, double *partials) {
@@ -89,8 +94,8 @@ multidot_kernel(const S *__restrict__ V, size_t ld, int m, const S *__restrict__
 template <typename S, int K>
 __global__ void __launch_bounds__(kT)
 residual_kernel(const S *__restrict__ V, const S *__restrict__ VA, size_t ld, int m,
-                const double *__restrict__ y, double theta, const double *__restrict__ diag, size_t n,
-                S *__restrict__ t, double *__restrict__ x_out, double *__restrict__ partials) {
+                const double *__restrict__ y, double theta, double pre_theta, const double *__restrict__ diag,
+                size_t n, S *__restrict__ t, double *__restrict__ x_out, double *__restrict__ partials) {
   __shared__ double ys[K];
   if (threadIdx.x < K) ys[threadIdx.x] = threadIdx.x < m ? y[threadIdx.x] : 0.0;
   __syncthreads();
@@ -111,7 +116,7 @@ residual_kernel(const S *__restrict__ V, const S *__restrict__ VA, size_t ld, in
     const double r = av - theta * xv;
     acc[0] += r * r;
     if (x_out) x_out[j] = xv;
-    const double d = fabs(diag[j] - theta);
+    const double d = fabs(diag[j] - pre_theta);
     const S ts = static_cast<S>(d > 1e-12 ? r / d : r / 1e-12);  // davidson.c:214-227
     t[j] = ts;
     const double td = static_cast<double>(ts);
@@ -211,6 +216,231 @@ combine_kernel(const S *__restrict__ V, size_t ld, int m, const double *__restri
 #pragma unroll
     for (int k = 0; k < K; ++k)
       if (k < m) s += static_cast<double>(V[k * ld + j]) * ys[k];
+    x[j] = s;
+  }
+}
+
+// ---- FP32-storage passes (the FP32 phase of the mixed mode) ---------------
+// Arithmetic in FP32 (GB300's FP64 rate is a small fraction of its FP32
+// rate, and these passes would be FP64-throughput bound); the operator is
+// shifted (H - lowest diagonal element), so the residual's cancellation is
+// mild.  Reductions add FP32 partial sums over kChunk elements of a thread
+// into FP64 accumulators, so sums over 10^8+ elements stay accurate.
+constexpr int kChunk = 16;
+
+// Per-thread FP64 accumulators kept in shared memory ([k][thread], so the
+// registers hold only the FP32 chunk sums); flushed once per chunk.  Up to 18
+// accumulators (37 KB per block; static shared memory stops at 48 KB); more
+// stay in registers (RegAcc).
+template <int NK>
+struct RegAcc {
+  double a[NK];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int k = 0; k < NK; ++k) a[k] = 0;
+  }
+  __device__ __forceinline__ void add(const float (&f)[NK], int nk) {
+#pragma unroll
+    for (int k = 0; k < NK; ++k)
+      if (k < nk) a[k] += f[k];
+  }
+  __device__ __forceinline__ void store(int nk, double *partials) { block_reduce_store<NK>(a, nk, partials); }
+};
+
+template <int NK>
+struct SmemAcc {
+  double *a;
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int k = 0; k < NK; ++k) a[k * kT + threadIdx.x] = 0;
+  }
+  __device__ __forceinline__ void add(const float (&f)[NK], int nk) {
+#pragma unroll
+    for (int k = 0; k < NK; ++k)
+      if (k < nk) a[k * kT + threadIdx.x] += f[k];
+  }
+  __device__ __forceinline__ void store(int nk, double *partials) {
+    double acc[NK];
+#pragma unroll
+    for (int k = 0; k < NK; ++k) acc[k] = k < nk ? a[k * kT + threadIdx.x] : 0.0;
+    block_reduce_store<NK>(acc, nk, partials);
+  }
+};
+
+template <int K>
+__global__ void __launch_bounds__(kT)
+multidot_f32_kernel(const float *__restrict__ V, size_t ld, int m, const float *__restrict__ w, size_t n,
+                    double *__restrict__ partials) {
+  __shared__ double acc_s[(K <= 16 ? K : 1) * kT];
+  typename std::conditional<K <= 16, SmemAcc<K>, RegAcc<K>>::type acc{};
+  if constexpr (K <= 16) acc.a = acc_s;
+  acc.zero();
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t j0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j0 < n; j0 += stride * kChunk) {
+    float f[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) f[k] = 0.f;
+#pragma unroll 4
+    for (int u = 0; u < kChunk; ++u) {
+      const size_t j = j0 + u * stride;
+      if (j >= n) break;
+      const float wj = w[j];
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (k < m) f[k] = fmaf(V[k * ld + j], wj, f[k]);
+    }
+    acc.add(f, m);
+  }
+  acc.store(m, partials);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kT)
+residual_f32_kernel(const float *__restrict__ V, const float *__restrict__ VA, size_t ld, int m,
+                    const double *__restrict__ y, double theta, double pre_theta, const double *__restrict__ diag,
+                    size_t n, float *__restrict__ t, double *__restrict__ x_out, double *__restrict__ partials) {
+  __shared__ float ys[K];
+  __shared__ double acc_s[(K <= 16 ? K + 2 : 1) * kT];
+  if (threadIdx.x < K) ys[threadIdx.x] = threadIdx.x < m ? static_cast<float>(y[threadIdx.x]) : 0.f;
+  typename std::conditional<K <= 16, SmemAcc<K + 2>, RegAcc<K + 2>>::type acc{};
+  if constexpr (K <= 16) acc.a = acc_s;
+  acc.zero();
+  __syncthreads();
+  const float th = static_cast<float>(theta);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t j0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j0 < n; j0 += stride * kChunk) {
+    float f[K + 2];
+#pragma unroll
+    for (int k = 0; k < K + 2; ++k) f[k] = 0.f;
+    for (int u = 0; u < kChunk; ++u) {
+      const size_t j = j0 + u * stride;
+      if (j >= n) break;
+      float v[K];
+      float xv = 0.f, av = 0.f;
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (k < m) {
+          v[k] = V[k * ld + j];
+          xv = fmaf(v[k], ys[k], xv);
+          av = fmaf(VA[k * ld + j], ys[k], av);
+        }
+      const float r = fmaf(-th, xv, av);
+      f[0] = fmaf(r, r, f[0]);
+      if (x_out) x_out[j] = xv;
+      const float d = fabsf(static_cast<float>(diag[j] - pre_theta));
+      const float ts = d > 1e-12f ? r / d : r / 1e-12f;  // davidson.c:214-227
+      t[j] = ts;
+      f[1] = fmaf(ts, ts, f[1]);
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (k < m) f[2 + k] = fmaf(v[k], ts, f[2 + k]);
+    }
+    acc.add(f, m + 2);
+  }
+  acc.store(m + 2, partials);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kT)
+gs_update_f32_kernel(const float *__restrict__ V, size_t ld, int m, const double *__restrict__ c, size_t n,
+                     float *__restrict__ t, double *__restrict__ partials) {
+  __shared__ float cs[K];
+  __shared__ double acc_s[(K <= 16 ? K + 1 : 1) * kT];
+  if (threadIdx.x < K) cs[threadIdx.x] = threadIdx.x < m ? static_cast<float>(c[threadIdx.x]) : 0.f;
+  typename std::conditional<K <= 16, SmemAcc<K + 1>, RegAcc<K + 1>>::type acc{};
+  if constexpr (K <= 16) acc.a = acc_s;
+  acc.zero();
+  __syncthreads();
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t j0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j0 < n; j0 += stride * kChunk) {
+    float f[K + 1];
+#pragma unroll
+    for (int k = 0; k < K + 1; ++k) f[k] = 0.f;
+    for (int u = 0; u < kChunk; ++u) {
+      const size_t j = j0 + u * stride;
+      if (j >= n) break;
+      float v[K];
+      float tv = t[j];
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (k < m) {
+          v[k] = V[k * ld + j];
+          tv = fmaf(-cs[k], v[k], tv);
+        }
+      t[j] = tv;
+      f[0] = fmaf(tv, tv, f[0]);
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (k < m) f[1 + k] = fmaf(v[k], tv, f[1 + k]);
+    }
+    acc.add(f, m + 1);
+  }
+  acc.store(m + 1, partials);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kT)
+gs_finish_f32_kernel(const float *__restrict__ V, size_t ld, int m, const double *__restrict__ c, double scale,
+                     size_t n, const float *__restrict__ t, float *__restrict__ out, double *__restrict__ partials) {
+  __shared__ float cs[K];
+  if (threadIdx.x < K) cs[threadIdx.x] = threadIdx.x < m ? static_cast<float>(c[threadIdx.x]) : 0.f;
+  __syncthreads();
+  const float sc = static_cast<float>(scale);
+  double acc[1] = {0};
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t j0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j0 < n; j0 += stride * kChunk) {
+    float f = 0.f;
+#pragma unroll 4
+    for (int u = 0; u < kChunk; ++u) {
+      const size_t j = j0 + u * stride;
+      if (j >= n) break;
+      float tv = t[j];
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (k < m) tv = fmaf(-cs[k], V[k * ld + j], tv);
+      const float o = tv * sc;
+      out[j] = o;
+      f = fmaf(o, o, f);
+    }
+    acc[0] += f;
+  }
+  block_reduce_store<1>(acc, 1, partials);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kT)
+deflate_f32_kernel(float *__restrict__ V, size_t ld, int mv, int keep, const double *__restrict__ Y, int ldy,
+                   size_t n) {
+  __shared__ float Ys[K * K];
+  for (int i = threadIdx.x; i < mv * keep; i += blockDim.x) Ys[i] = static_cast<float>(Y[(i / mv) * ldy + (i % mv)]);
+  __syncthreads();
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    float v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < mv) v[k] = V[k * ld + j];
+    for (int cc = 0; cc < keep; ++cc) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (k < mv) s = fmaf(v[k], Ys[cc * mv + k], s);
+      V[cc * ld + j] = s;
+    }
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kT)
+combine_f32_kernel(const float *__restrict__ V, size_t ld, int m, const double *__restrict__ y, size_t n,
+                   double *__restrict__ x) {
+  __shared__ float ys[K];
+  if (threadIdx.x < K) ys[threadIdx.x] = threadIdx.x < m ? static_cast<float>(y[threadIdx.x]) : 0.f;
+  __syncthreads();
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (k < m) s = fmaf(V[k * ld + j], ys[k], s);
     x[j] = s;
   }
 }
@@ -366,39 +596,63 @@ int dispatch_k(int m, cudaStream_t st, Args... args) {
 template <typename S, int K>
 struct MultidotL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const S *w, size_t n, double *p) {
+    if constexpr (std::is_same<S, float>::value)
+      multidot_f32_kernel<K><<<g, kT, 0, st>>>(V, ld, m, w, n, p);
+    else
+      multidot_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, w, n, p);
+  }
+};
+template <typename S, int K>
+struct MultidotExactL {
+  static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const S *w, size_t n, double *p) {
     multidot_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, w, n, p);
   }
 };
 template <typename S, int K>
 struct ResidualL {
   static void run(int g, cudaStream_t st, const S *V, const S *VA, size_t ld, int m, const double *y, double th,
-                  const double *diag, size_t n, S *t, double *x, double *p) {
-    residual_kernel<S, K><<<g, kT, 0, st>>>(V, VA, ld, m, y, th, diag, n, t, x, p);
+                  double pre, const double *diag, size_t n, S *t, double *x, double *p) {
+    if constexpr (std::is_same<S, float>::value)
+      residual_f32_kernel<K><<<g, kT, 0, st>>>(V, VA, ld, m, y, th, pre, diag, n, t, x, p);
+    else
+      residual_kernel<S, K><<<g, kT, 0, st>>>(V, VA, ld, m, y, th, pre, diag, n, t, x, p);
   }
 };
 template <typename S, int K>
 struct GsUpdateL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *p) {
-    gs_update_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, c, n, t, p);
+    if constexpr (std::is_same<S, float>::value)
+      gs_update_f32_kernel<K><<<g, kT, 0, st>>>(V, ld, m, c, n, t, p);
+    else
+      gs_update_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, c, n, t, p);
   }
 };
 template <typename S, int K>
 struct GsFinishL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, double sc, size_t n,
                   const S *t, S *out, double *p) {
-    gs_finish_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, c, sc, n, t, out, p);
+    if constexpr (std::is_same<S, float>::value)
+      gs_finish_f32_kernel<K><<<g, kT, 0, st>>>(V, ld, m, c, sc, n, t, out, p);
+    else
+      gs_finish_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, c, sc, n, t, out, p);
   }
 };
 template <typename S, int K>
 struct DeflateL {
   static void run(int g, cudaStream_t st, S *V, size_t ld, int mv, int keep, const double *Y, int ldy, size_t n) {
-    deflate_kernel<S, K><<<g, kT, 0, st>>>(V, ld, mv, keep, Y, ldy, n);
+    if constexpr (std::is_same<S, float>::value)
+      deflate_f32_kernel<K><<<g, kT, 0, st>>>(V, ld, mv, keep, Y, ldy, n);
+    else
+      deflate_kernel<S, K><<<g, kT, 0, st>>>(V, ld, mv, keep, Y, ldy, n);
   }
 };
 template <typename S, int K>
 struct CombineL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *y, size_t n, double *x) {
-    combine_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, y, n, x);
+    if constexpr (std::is_same<S, float>::value)
+      combine_f32_kernel<K><<<g, kT, 0, st>>>(V, ld, m, y, n, x);
+    else
+      combine_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, y, n, x);
   }
 };
 
@@ -408,6 +662,19 @@ int vec_partials_capacity() { return grid_blocks() * kMaxK; }
 
 int vec_reduction_blocks() { return grid_blocks(); }
 
+namespace {
+__global__ void shifted_diag_kernel(const double *__restrict__ d, double shift, float *__restrict__ out, size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    out[j] = static_cast<float>(d[j] - shift);
+}
+}  // namespace
+
+int vec_shifted_diag32(const double *d, double shift, float *out, size_t n, cudaStream_t st) {
+  shifted_diag_kernel<<<grid_blocks(), kT, 0, st>>>(d, shift, out, n);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
 int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st) {
   reduce_partials_kernel<<<1, kT, 0, st>>>(partials, grid_blocks(), nk, out);
   DOCI_CUDA(cudaGetLastError());
@@ -415,15 +682,17 @@ int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st) {
 }
 
 template <typename S>
-int vec_multidot(const S *V, size_t ld, int m, const S *w, size_t n, double *partials, cudaStream_t st) {
+int vec_multidot(const S *V, size_t ld, int m, const S *w, size_t n, double *partials, cudaStream_t st,
+                 bool fp64_products) {
   if (m < 1 || m > 32) return DOCI_ERR_INVALID;
+  if (fp64_products) return dispatch_k<S, MultidotExactL>(m, st, V, ld, m, w, n, partials);
   return dispatch_k<S, MultidotL>(m, st, V, ld, m, w, n, partials);
 }
 template <typename S>
 int vec_residual(const S *V, const S *VA, size_t ld, int m, const double *y, double theta, const double *diag,
-                 size_t n, S *t, double *x, double *partials, cudaStream_t st) {
+                 size_t n, S *t, double *x, double *partials, cudaStream_t st, double diag_shift) {
   if (m < 1 || m > 32) return DOCI_ERR_INVALID;
-  return dispatch_k<S, ResidualL>(m, st, V, VA, ld, m, y, theta, diag, n, t, x, partials);
+  return dispatch_k<S, ResidualL>(m, st, V, VA, ld, m, y, theta, theta + diag_shift, diag, n, t, x, partials);
 }
 template <typename S>
 int vec_gs_update(const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *partials, cudaStream_t st) {
@@ -514,9 +783,9 @@ int precond_inverse(const double *diag, double *pinv, size_t n, cudaStream_t st)
 }
 
 #define DOCI_VEC_INST(S)                                                                                   \
-  template int vec_multidot<S>(const S *, size_t, int, const S *, size_t, double *, cudaStream_t);          \
+  template int vec_multidot<S>(const S *, size_t, int, const S *, size_t, double *, cudaStream_t, bool);    \
   template int vec_residual<S>(const S *, const S *, size_t, int, const double *, double, const double *,   \
-                               size_t, S *, double *, double *, cudaStream_t);                              \
+                               size_t, S *, double *, double *, cudaStream_t, double);                      \
   template int vec_gs_update<S>(const S *, size_t, int, const double *, size_t, S *, double *, cudaStream_t); \
   template int vec_gs_finish<S>(const S *, size_t, int, const double *, double, size_t, const S *, S *,      \
                                 double *, cudaStream_t);                                                    \

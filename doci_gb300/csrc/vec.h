@@ -15,10 +15,15 @@ int vec_reduction_blocks();
 int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st);
 
 template <typename S>
-int vec_multidot(const S *V, size_t ld, int m, const S *w, size_t n, double *partials, cudaStream_t st);
+int vec_multidot(const S *V, size_t ld, int m, const S *w, size_t n, double *partials, cudaStream_t st,
+                 bool fp64_products = false);  // FP32 storage: true = exact products, FP64 sums
 template <typename S>
 int vec_residual(const S *V, const S *VA, size_t ld, int m, const double *y, double theta, const double *diag,
-                 size_t n, S *t, double *x, double *partials, cudaStream_t st);
+                 size_t n, S *t, double *x, double *partials, cudaStream_t st, double diag_shift = 0.0);
+// index of the smallest element (first on ties), synchronous
+int vec_argmin(const double *d, size_t n, int64_t *idx, cudaStream_t st);
+// out[j] = (float)(d[j] - shift): the FP32 diagonal of the shifted operator H - shift
+int vec_shifted_diag32(const double *d, double shift, float *out, size_t n, cudaStream_t st);
 template <typename S>
 int vec_gs_update(const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *partials, cudaStream_t st);
 template <typename S>

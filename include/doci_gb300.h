@@ -207,8 +207,12 @@ typedef enum doci_solver_kind { DOCI_SOLVER_D = 0, DOCI_SOLVER_CG = 1, DOCI_SOLV
 
 typedef enum doci_solve_mode {
   DOCI_MODE_FP64 = 0,  /* FP64 sigma and FP64 basis throughout */
-  DOCI_MODE_MIXED = 1  /* FP32 sigma and FP32 basis (FP64 reductions, GS, residual,
-                          subspace), then FP64 Davidson steps from that vector */
+  DOCI_MODE_MIXED = 1  /* FP32 phase: FP32 sigma and FP32 basis on the shifted
+                          operator H - (lowest diagonal element), FP32 vector
+                          arithmetic with FP64 accumulation of the reductions,
+                          FP64 subspace eigenproblem; it ends at mixed_tol or
+                          when the residual stops improving.  Then FP64
+                          Davidson steps from that vector to tol. */
 } doci_solve_mode;
 
 typedef struct doci_solve_opts {

@@ -36,6 +36,7 @@ def test_noalloc_matches_multidot_twice(lib, dtype, prec):
     ref = torch.empty(m, dtype=torch.float64, device="cuda")
     out = torch.full((m,), float("nan"), dtype=torch.float64, device="cuda")
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # V, w, out were written on the default stream
     with torch.cuda.stream(s):
         assert lib.doci_multidot(C.c_void_p(V.data_ptr()), n, m, C.c_void_p(w.data_ptr()), n, prec,
                                  C.c_void_p(ref.data_ptr()), C.c_void_p(s.cuda_stream)) == 0
