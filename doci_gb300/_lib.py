@@ -58,7 +58,8 @@ class SolveResult(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("nroots", C.c_int), ("max_vec", C.c_int), ("max_its", C.c_int), ("tol", C.c_double),
-                ("mode", C.c_int), ("mixed_tol", C.c_double), ("workers", C.c_int), ("hbm_budget", C.c_int64)]
+                ("mode", C.c_int), ("mixed_tol", C.c_double), ("workers", C.c_int), ("hbm_budget", C.c_int64),
+                ("keep", C.c_int)]
 
 
 class RootResult(C.Structure):

@@ -271,6 +271,8 @@ typedef struct doci_batch_opts {
   double mixed_tol;    /* residual at which the FP32 phase hands over (1e-4) */
   int workers;         /* solves in flight at once, one CUDA stream each (8) */
   int64_t hbm_budget;  /* device bytes the solves in flight may hold; 0 = 85% of free */
+  int keep;            /* basis vectors kept at a thick restart, nroots..max_vec - nroots;
+                          0 = automatic (max(2 nroots, max_vec / 4)) */
 } doci_batch_opts;
 
 typedef struct doci_root_result {
