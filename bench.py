@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge measurement")
-    ap.add_argument("--workload", choices=["sigma", "batch", "serve"], default="sigma",
+    ap.add_argument("--workload", choices=["sigma", "batch", "serve", "solve"], default="sigma",
                     help="sigma: the headline sigma benchmark; batch: many Hamiltonians, several roots; "
                          "serve: Poisson request stream through the request server")
     ap.add_argument("--problems", type=int, default=256, help="batch: number of Hamiltonians")
@@ -72,6 +72,9 @@ def parse():
     ap.add_argument("--lmin", type=int, default=None)
     ap.add_argument("--lmax", type=int, default=None)
     ap.add_argument("--max-vec", type=int, default=16, help="DAVIDSON_MAX_VEC of the convergence runs")
+    ap.add_argument("--mode", choices=["mixed", "fp64"], default="mixed", help="solve: precision mode")
+    ap.add_argument("--max-its", type=int, default=200, help="solve: iteration limit")
+    ap.add_argument("--tol", type=float, default=1e-7, help="solve: residual tolerance")
     ap.add_argument("--mixed-tol", type=float, default=1e-4,
                     help="residual that ends the FP32 phase of the time-to-converge run")
     return ap.parse_args()
@@ -335,6 +338,23 @@ def serve_workload(a):
     print(json.dumps(line), flush=True)
 
 
+def solve_workload(a):
+    """One Davidson solve of the sigma workload's Hamiltonian through the
+    public solve_trace: iterations, energy and wall time (a profiling target
+    for the solver's vector passes)."""
+    import doci_gb300 as dg
+    path = workload_path(a.L, a.N, a.seed, 0, 1)
+    with dg.Hamiltonian.from_fcidump(path) as h:
+        r, _, tr = h.solve_trace(solver="D", davidson_max_vec=a.max_vec, davidson_keep=2, max_its=a.max_its,
+                                 tol=a.tol, mode=a.mode, mixed_tol=a.mixed_tol)
+    line = {"metric": "Davidson solve wall time", "value": float(tr[-1, 3]) if len(tr) else None, "unit": "s",
+            "higher_is_better": False, "impl": "ours", "energy": r["energy"], "residual": r["residual"],
+            "iterations": r["iterations"], "iterations_fp32": r["iterations_fp32"],
+            "config": {"workload": f"Davidson L={a.L} N={a.N} seed={a.seed} mode={a.mode} max_vec={a.max_vec} "
+                                   f"tol={a.tol} mixed_tol={a.mixed_tol} max_its={a.max_its}"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
     ws, rank, local = dist_env()
@@ -344,6 +364,8 @@ def main():
         return batch_workload(a)
     if a.workload == "serve":
         return serve_workload(a)
+    if a.workload == "solve":
+        return solve_workload(a)
     import numpy as np
     import torch
     import doci_gb300 as dg
