@@ -338,6 +338,9 @@ def serve_workload(a):
     print(json.dumps(line), flush=True)
 
 
+KERNEL_NAMES = {1: "gather", 2: "row", 3: "row1", 4: "rowx", 5: "rowxc", 6: "pair"}
+
+
 def solve_workload(a):
     """One Davidson solve of the sigma workload's Hamiltonian through the
     public solve_trace: iterations, energy and wall time (a profiling target
@@ -389,6 +392,10 @@ def main():
     torch.cuda.synchronize()
     if nv > 1:  # a block of vectors per step: the device-timed figure only
         a.no_e2e = a.no_converge = True
+
+    plan_kind, plan_launches = h.sigma_plan(prec)
+    # kernel launches of one step: doci_sigma's plan, or the block sigma's groups of up to 4 vectors
+    launches_per_step = plan_launches if nv == 1 else (nv + 3) // 4
 
     def step():
         if nv == 1:
@@ -477,7 +484,8 @@ def main():
                            "L": a.L, "N": a.N, "D": D, "seed": a.seed, "precision": a.precision,
                            "l2": "inputs larger than L2 (x and sigma are D*4 B = %.2f GB each)" % (D * esize / 1e9),
                            "parallelism": f"replicas x{ws}"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": a.steps * ((nv + 3) // 4),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": a.steps * launches_per_step,
+                "sigma_kernel": KERNEL_NAMES.get(plan_kind, plan_kind),
                 "clocks": clk, "time_to_converge": conv, "impl": "ours"}
         print(json.dumps(line), flush=True)
     h.close()

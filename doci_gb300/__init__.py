@@ -8,10 +8,10 @@ FCIDUMP generator used by the benchmark workloads.
 """
 from ._lib import (FP32, FP64, MODE_FP64, MODE_MIXED, SOLVER_CG, SOLVER_CGP,  # noqa: F401
                    SOLVER_D, DociError, Hamiltonian, LIB_PATH, Server, SolveOpts, SolveResult, batch_opts,
-                   batch_solve, default_opts, footprint, lib, solve_roots)
+                   batch_solve, default_opts, fcidump_integrals, footprint, lib, solve_roots)
 from .fcidump import raw_integrals, synthetic_integrals, write_fcidump, write_synthetic_fcidump  # noqa: F401
 
 __all__ = ["FP32", "FP64", "MODE_FP64", "MODE_MIXED", "SOLVER_D", "SOLVER_CG", "SOLVER_CGP", "DociError",
            "Hamiltonian", "LIB_PATH", "Server", "SolveOpts", "SolveResult", "batch_opts", "batch_solve",
-           "default_opts", "footprint", "lib", "solve_roots",
+           "default_opts", "fcidump_integrals", "footprint", "lib", "solve_roots",
            "raw_integrals", "synthetic_integrals", "write_fcidump", "write_synthetic_fcidump"]

@@ -95,6 +95,9 @@ def lib() -> C.CDLL:
     sig = {
         "doci_status_string": (C.c_char_p, [i]),
         "doci_ham_from_fcidump": (i, [C.c_char_p, C.POINTER(vp)]),
+        "doci_ham_from_fcidump_relaxed": (i, [C.c_char_p, C.POINTER(vp)]),
+        "doci_fcidump_integrals": (i, [C.c_char_p, i, C.POINTER(i), C.POINTER(i), C.POINTER(i), pd, pd, pd,
+                                       C.POINTER(i)]),
         "doci_ham_from_integrals": (i, [i, i, d, pd, pd, C.POINTER(vp)]),
         "doci_ham_destroy": (None, [vp]),
         "doci_ham_dims": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i64)]),
@@ -102,6 +105,7 @@ def lib() -> C.CDLL:
         "doci_ham_diagonal_device": (vp, [vp]),
         "doci_sigma": (i, [vp, vp, vp, i, vp]),
         "doci_sigma_block": (i, [vp, vp, C.c_int64, vp, C.c_int64, i, i, vp]),
+        "doci_sigma_plan": (i, [vp, i, C.POINTER(i), C.POINTER(i)]),
         "doci_sigma_host": (i, [vp, vp, vp, i]),
         "doci_ham_set_sigma_kernel": (i, [vp, i]),
         "doci_bitstrings": (i, [vp, i64, i64, vp, vp]),
@@ -173,9 +177,12 @@ class Hamiltonian:
         self.L, self.N, self.D = L.value, N.value, D.value
 
     @classmethod
-    def from_fcidump(cls, path: str) -> "Hamiltonian":
+    def from_fcidump(cls, path: str, relaxed: bool = False) -> "Hamiltonian":
+        """relaxed=True: the relaxed reader (any namelist layout and integral
+        index order); default: the reference's reader."""
         h = C.c_void_p()
-        _check(lib().doci_ham_from_fcidump(os.fsencode(path), C.byref(h)), f"doci_ham_from_fcidump({path})")
+        fn = lib().doci_ham_from_fcidump_relaxed if relaxed else lib().doci_ham_from_fcidump
+        _check(fn(os.fsencode(path), C.byref(h)), f"doci_ham_from_fcidump({path})")
         return cls(h.value)
 
     @classmethod
@@ -236,6 +243,13 @@ class Hamiltonian:
         _check(lib().doci_sigma(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), precision,
                                 C.c_void_p(stream or None)), "doci_sigma")
 
+    def sigma_plan(self, precision: int = FP64):
+        """(kind, launches) of doci_sigma on this handle: the kernel the
+        automatic choice resolves to and the kernel launches per call."""
+        k, n = C.c_int(), C.c_int()
+        _check(lib().doci_sigma_plan(self._h, precision, C.byref(k), C.byref(n)), "doci_sigma_plan")
+        return k.value, n.value
+
     def sigma_block_device(self, x_ptr: int, ldx: int, y_ptr: int, ldy: int, nv: int, precision: int = FP64,
                            stream: int = 0) -> None:
         """Block sigma over nv column-major vectors on device buffers."""
@@ -274,6 +288,21 @@ class Hamiltonian:
         _check(lib().doci_solve_trace(self._h, C.byref(o), _dptr(v), C.byref(r), _dptr(tr), max_records,
                                       C.byref(n)), "doci_solve_trace")
         return r.as_dict(), v, tr[:n.value].copy()
+
+
+def fcidump_integrals(path: str, relaxed: bool = False) -> dict:
+    """Raw integrals of an FCIDUMP (before the transform) by the reference's
+    reader or the relaxed one; host only (no GPU needed)."""
+    L, na, nb, bad = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    core = C.c_double()
+    p = os.fsencode(path)
+    _check(lib().doci_fcidump_integrals(p, int(relaxed), C.byref(L), C.byref(na), C.byref(nb), C.byref(core),
+                                        None, None, C.byref(bad)), f"doci_fcidump_integrals({path})")
+    one = np.zeros(L.value ** 2)
+    two = np.zeros(L.value ** 4)
+    _check(lib().doci_fcidump_integrals(p, int(relaxed), None, None, None, None, _dptr(one), _dptr(two),
+                                        C.byref(bad)), f"doci_fcidump_integrals({path})")
+    return {"L": L.value, "n_alpha": na.value, "n_beta": nb.value, "core": core.value, "one": one, "two": two}
 
 
 def batch_opts(**kw) -> BatchOpts:

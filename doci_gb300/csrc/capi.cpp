@@ -128,6 +128,33 @@ int doci_ham_from_fcidump(const char *path, doci_ham **out) {
   return build_from_integrals(in, out);
 }
 
+int doci_ham_from_fcidump_relaxed(const char *path, doci_ham **out) {
+  if (!path || !out) return DOCI_ERR_INVALID;
+  *out = nullptr;
+  Integrals in;
+  int bad = 0;
+  const int st = read_fcidump_relaxed(path, &in, &bad);
+  if (st) return st;
+  return build_from_integrals(in, out);
+}
+
+int doci_fcidump_integrals(const char *path, int relaxed, int *L, int *n_alpha, int *n_beta, double *core,
+                           double *one, double *two, int *bad_line) {
+  if (!path) return DOCI_ERR_INVALID;
+  Integrals in;
+  int bad = 0;
+  const int st = relaxed ? read_fcidump_relaxed(path, &in, &bad) : read_fcidump_file(path, &in, &bad);
+  if (bad_line) *bad_line = bad;
+  if (st) return st;
+  if (L) *L = in.L;
+  if (n_alpha) *n_alpha = in.Na;
+  if (n_beta) *n_beta = in.Nb;
+  if (core) *core = in.core;
+  if (one) std::memcpy(one, in.one.data(), in.one.size() * sizeof(double));
+  if (two) std::memcpy(two, in.two.data(), in.two.size() * sizeof(double));
+  return DOCI_OK;
+}
+
 int doci_ham_from_integrals(int L, int n_pairs, double core, const double *one, const double *two,
                             doci_ham **out) {
   if (!out || !one || !two || L < 1 || n_pairs < 0) return DOCI_ERR_INVALID;
@@ -190,6 +217,14 @@ int doci_sigma_block(doci_ham *h, const void *d_X, int64_t ldx, void *d_Y, int64
                                      y + v0 * static_cast<size_t>(ldy) * es, ldy, k, precision, st);
     if (r != DOCI_OK) return r;
   }
+  return DOCI_OK;
+}
+
+int doci_sigma_plan(const doci_ham *h, int precision, int *kind, int *launches) {
+  if (!h || (precision != DOCI_FP64 && precision != DOCI_FP32)) return DOCI_ERR_INVALID;
+  const SigmaPlan p = plan_sigma(h, precision);
+  if (kind) *kind = p.kind;
+  if (launches) *launches = p.launches;
   return DOCI_OK;
 }
 

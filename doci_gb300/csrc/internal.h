@@ -30,6 +30,9 @@ struct Integrals {
 // FCIDUMP reader restating read_fcidump.c:18-82; returns a doci_status and
 // the offending line number on a format error.
 int read_fcidump_file(const char *path, Integrals *out, int *bad_line);
+// relaxed reader (fcidump.cpp): multi-line namelist, any key order, other
+// keys ignored, any integral index order (stored canonically)
+int read_fcidump_relaxed(const char *path, Integrals *out, int *bad_line);
 // doci.c:630-665 (in place)
 void transform_integrals(double *one, double *two, int L);
 // doci.c:687-701
@@ -117,6 +120,12 @@ int ham_build(doci_ham *h, const Integrals &in);
 void ham_release(doci_ham *h);
 int ham_stage(doci_ham *h, size_t bytes);
 // sigma.cu
+// The kernel path of a sigma: kind as doci_ham_set_sigma_kernel (1..6) and
+// the number of kernel launches it takes.
+struct SigmaPlan {
+  int kind, launches;
+};
+SigmaPlan plan_sigma(const doci_ham *h, int precision, bool allow_pair = true);
 // allow_pair = false keeps the FP32 result run-to-run reproducible (the pair
 // form adds with atomics)
 int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t s, bool allow_pair = true);

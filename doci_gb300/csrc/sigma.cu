@@ -881,36 +881,50 @@ unsigned grid_for(uint64_t n) {
 
 }  // namespace
 
-int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t st, bool allow_pair) {
-  if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
+SigmaPlan plan_sigma(const doci_ham *h, int precision, bool allow_pair) {
   const size_t elem = precision == DOCI_FP64 ? 8 : 4;
   // pair form: on request (kind 6), and the automatic FP32 choice when its
   // blocks give every SM work (measured fastest there); FP32 only
   const bool want_pair = h->sigma_kernel == 6 || (h->sigma_kernel == 0 && h->npblocks >= device_sm_count());
-  if (allow_pair && want_pair && precision == DOCI_FP32 && pair_fits(h))
-    return launch_pair(h, static_cast<const float *>(x), static_cast<float *>(y), st);
+  if (allow_pair && want_pair && precision == DOCI_FP32 && pair_fits(h)) return {6, 2};  // init pass + pair pass
   // row kernel when the row tiling exists, fits, and gives every SM work
   bool row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
-  if (!row) return precision == DOCI_FP64 ? launch_typed<double>(h, x, y, st) : launch_typed<float>(h, x, y, st);
+  if (!row) return {1, 1};
   // automatic: the phase-ordered pass for FP64 (measured faster there), the
   // single row pass for FP32 (measured faster there)
   const bool want_rowx = h->sigma_kernel >= 4 || (h->sigma_kernel == 0 && precision == DOCI_FP64);
   if (want_rowx && rowx_fits(h, elem)) {
-    // phase-ordered row pass; kind 5 moves the row-part hops to the column pass
+    // kind 5 moves the row-part hops to the column-panel pass
     const bool colp = h->sigma_kernel == 5 && col_pass_fits(h, elem);
-    int r = precision == DOCI_FP64 ? launch_rowx<double>(h, x, y, st, colp ? 0 : 1)
-                                   : launch_rowx<float>(h, x, y, st, colp ? 0 : 1);
-    if (r || !colp) return r;
-    return precision == DOCI_FP64 ? launch_col<double>(h, x, y, st) : launch_col<float>(h, x, y, st);
+    return colp ? SigmaPlan{5, 2} : SigmaPlan{4, 1};
   }
   // row-part hops in the column-panel pass only on request (kind 2): the
   // single row pass (kind 3, and the automatic choice) measured faster
   const bool col = h->sigma_kernel == 2 && col_pass_fits(h, elem);
-  int r = precision == DOCI_FP64 ? launch_row<double>(h, x, y, st, col ? 0 : 1)
-                                 : launch_row<float>(h, x, y, st, col ? 0 : 1);
-  if (r || !col) return r;
-  return precision == DOCI_FP64 ? launch_col<double>(h, x, y, st) : launch_col<float>(h, x, y, st);
+  return col ? SigmaPlan{2, 2} : SigmaPlan{3, 1};
+}
+
+int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t st, bool allow_pair) {
+  if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
+  const bool f64 = precision == DOCI_FP64;
+  const SigmaPlan p = plan_sigma(h, precision, allow_pair);
+  int r = DOCI_OK;
+  switch (p.kind) {
+    case 6:
+      return launch_pair(h, static_cast<const float *>(x), static_cast<float *>(y), st);
+    case 1:
+      return f64 ? launch_typed<double>(h, x, y, st) : launch_typed<float>(h, x, y, st);
+    case 4:
+    case 5:
+      r = f64 ? launch_rowx<double>(h, x, y, st, p.kind == 5 ? 0 : 1) : launch_rowx<float>(h, x, y, st, p.kind == 5 ? 0 : 1);
+      break;
+    default:  // 2, 3
+      r = f64 ? launch_row<double>(h, x, y, st, p.kind == 2 ? 0 : 1) : launch_row<float>(h, x, y, st, p.kind == 2 ? 0 : 1);
+      break;
+  }
+  if (r || p.launches == 1) return r;
+  return f64 ? launch_col<double>(h, x, y, st) : launch_col<float>(h, x, y, st);
 }
 
 int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv, int precision,

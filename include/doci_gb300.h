@@ -117,6 +117,24 @@ const char *doci_status_string(int status);
  * reference: read_fcidump.c:18-82, doci.c:630-665). */
 int doci_ham_from_fcidump(const char *path, doci_ham **out);
 
+/* Build from an FCIDUMP file read by the relaxed reader (no counterpart in
+ * the reference, whose reader wants the header on one line in a fixed order
+ * and propagates the 8-fold symmetry only from canonically ordered entries):
+ * the &FCI ... &END (or /) namelist over any number of lines, keys in any
+ * order and case, other keys (ORBSYM, ISYM, UHF, ...) ignored, MS2 optional
+ * (0), Fortran D exponents, blank lines; every integral entry is stored at
+ * its canonical slot whatever its index order, so the transform sees it.
+ * Two entries naming the same integral with different values are a format
+ * error.  On canonically ordered files it gives the reference's integrals. */
+int doci_ham_from_fcidump_relaxed(const char *path, doci_ham **out);
+
+/* Host-only: the raw integrals of an FCIDUMP (before the transform, layout of
+ * doci_ham_from_integrals) by the reference's reader (relaxed = 0) or the
+ * relaxed one (1).  one/two may be NULL (dimensions only); else they hold
+ * L*L and L^4 doubles.  *bad_line gets the offending line of a format error. */
+int doci_fcidump_integrals(const char *path, int relaxed, int *L, int *n_alpha, int *n_beta, double *core,
+                           double *one, double *two, int *bad_line);
+
 /* Build from integrals laid out as read_fcidump returns them (before the
  * transform): one[L*L], two[L^4] with two[i + j L + k L^2 + l L^3] = (ij|kl),
  * 0-based, canonical entries at least (the transform mirrors them). */
@@ -163,6 +181,11 @@ int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int
  * runs; FP64 requests use the automatic choice).  2-6 fall back to 1 when
  * the handle has no row tiling.  For tests and tuning. */
 int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
+
+/* The path doci_sigma takes for this handle and precision: *kind as in
+ * doci_ham_set_sigma_kernel (1..6; the automatic choice resolved) and
+ * *launches, the number of kernel launches of one call.  Host-only query. */
+int doci_sigma_plan(const doci_ham *ham, int precision, int *kind, int *launches);
 
 /* Same on host buffers; copies in and out inside the call, synchronous. */
 int doci_sigma_host(doci_ham *ham, const void *x, void *y, int precision);

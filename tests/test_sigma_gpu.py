@@ -207,3 +207,22 @@ def test_sigma_block_vs_oracle(L, N, seed, nv, kernel, synth, dg):
                 assert np.abs(y - ys).max() <= tol * np.abs(refs[v]).max()
                 if kernel in ("gather", "row1"):  # same kernel family: same summation order
                     assert np.array_equal(y, ys)
+
+
+def test_sigma_plan(synth, dg):
+    """doci_sigma_plan reports the path doci_sigma takes: the automatic choice
+    resolves to the pair form (2 launches) for FP32 and the phase-ordered row
+    pass for FP64 once the tilings give every SM work, the gather kernel on
+    small spaces; an explicit kind is honoured."""
+    with dg.Hamiltonian.from_fcidump(synth(20, 10, 51)) as h:
+        assert h.sigma_plan(dg.FP32) == (6, 2)
+        assert h.sigma_plan(dg.FP64) == (4, 1)
+        h.set_sigma_kernel("row1")
+        assert h.sigma_plan(dg.FP32) == (3, 1)
+        h.set_sigma_kernel("rowxc")
+        assert h.sigma_plan(dg.FP64) == (5, 2)
+        h.set_sigma_kernel("pair")
+        assert h.sigma_plan(dg.FP64) == (4, 1)  # FP32 only
+    with dg.Hamiltonian.from_fcidump(synth(12, 6, 52)) as h:
+        assert h.sigma_plan(dg.FP32) == (1, 1)
+        assert h.sigma_plan(dg.FP64) == (1, 1)
