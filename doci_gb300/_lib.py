@@ -41,7 +41,7 @@ class SolveOpts(C.Structure):
         ("solver", C.c_int), ("max_its", C.c_int), ("tol", C.c_double),
         ("davidson_keep", C.c_int), ("davidson_max_vec", C.c_int), ("hf_init", C.c_int),
         ("mode", C.c_int), ("mixed_tol", C.c_double), ("print_level", C.c_int),
-        ("seed", C.c_uint64),
+        ("seed", C.c_uint64), ("fp32_corrections", C.c_int),
     ]
 
 

@@ -90,6 +90,36 @@ int make_start(doci_ham *h, int hf_init, uint64_t seed, double *d_t, cudaStream_
   return vec_fill_random(d_t, h->D, seed, st);
 }
 
+// One FP64 sigma y = H x (through op, as an anchor), theta = x.y / x.x and
+// the residual norm ||y - theta x|| / ||x||.  dp: partial-sum scratch of
+// vec_partials_capacity() + 64 doubles; r: D doubles of scratch.
+int fp64_check(MatvecOp &op, const double *d_x, size_t D, double *d_y, double *d_r, double *dp, cudaStream_t st,
+               double *theta, double *rnorm) {
+  op.anchor_next = true;
+  int s = op.apply(d_x, d_y, DOCI_FP64, st);
+  if (s) return s;
+  double *d_red = dp + vec_partials_capacity();
+  double h_red[3];
+  if ((s = vec_multidot<double>(d_x, D, 1, d_y, D, dp, st))) return s;
+  if ((s = vec_reduce(dp, 1, d_red, st))) return s;
+  if ((s = vec_multidot<double>(d_x, D, 1, d_x, D, dp, st))) return s;
+  if ((s = vec_reduce(dp, 1, d_red + 1, st))) return s;
+  DOCI_CUDA(cudaMemcpyAsync(h_red, d_red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DOCI_CUDA(cudaStreamSynchronize(st));
+  const double xx = h_red[1] > 0 ? h_red[1] : 1.0;
+  *theta = h_red[0] / xx;
+  // r = y - theta x with the residual pass (coefficient 1 on x and y)
+  const double one = 1.0;
+  DOCI_CUDA(cudaMemcpyAsync(d_red + 8, &one, sizeof(double), cudaMemcpyHostToDevice, st));
+  if ((s = vec_residual<double>(d_x, d_y, D, 1, d_red + 8, *theta, op.ham->d_diag, D, d_r, nullptr, dp, st)))
+    return s;
+  if ((s = vec_reduce(dp, 3, d_red + 16, st))) return s;
+  DOCI_CUDA(cudaMemcpyAsync(h_red, d_red + 16, sizeof(double), cudaMemcpyDeviceToHost, st));
+  DOCI_CUDA(cudaStreamSynchronize(st));
+  *rnorm = std::sqrt(h_red[0] / xx);
+  return DOCI_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -288,6 +318,7 @@ void doci_solve_opts_default(doci_solve_opts *o) {
   o->hf_init = 1;
   o->mode = DOCI_MODE_FP64;
   o->mixed_tol = 1e-5;
+  o->fp32_corrections = 1;
   o->print_level = 0;
   o->seed = 1;
 }
@@ -307,8 +338,11 @@ int64_t doci_solve_footprint(int L, int n_pairs, const doci_solve_opts *o, int n
   if (o->solver != DOCI_SOLVER_D) {
     solver = D * 8 * 7;  // x, p, Ax, Ap, g, pinv + start
   } else if (o->mode == DOCI_MODE_MIXED) {
-    // FP32 phase: basis, start, x, shifted FP32 diagonal
-    const int64_t p32 = D * (2 * mv * 4 + 4 + 8 + 4), p64 = D * (2 * mv * 8 + 8 + 8);
+    // FP32 phase: basis, start, x, shifted FP32 diagonal; FP64 phase: basis,
+    // start, x, and with FP32 corrections the shifted diagonal, two FP32 and
+    // two FP64 scratch vectors
+    const int64_t p32 = D * (2 * mv * 4 + 4 + 8 + 4);
+    const int64_t p64 = D * (2 * mv * 8 + 8 + 8 + (o->fp32_corrections ? 4 + 8 + 16 : 0));
     solver = p32 > p64 ? p32 : p64;
   } else {
     solver = D * (2 * mv * 8 + 8 + 8);
@@ -392,12 +426,54 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
     a.max_its = its_left;
     DevBuf t;
     t.st = st;
-  DOCI_CUDA(cudaMallocAsync(&t.p, sizeof(double) * D, st));
+    DOCI_CUDA(cudaMallocAsync(&t.p, sizeof(double) * D, st));
     DOCI_CUDA(cudaMemcpyAsync(t.p, d_x, sizeof(double) * D, cudaMemcpyDeviceToDevice, st));
-    if ((s = davidson_run<double>(op, D, h->d_diag, static_cast<double *>(t.p), a, st, &out, d_x))) return s;
+    // mixed mode: the FP64 phase computes the correction vectors' sigmas in
+    // FP32 on the shifted view (each run's first sigma, the anchor, and a
+    // closing verification sigma are FP64); plain FP64 mode: FP64 throughout
+    const bool corr32 = o.mode == DOCI_MODE_MIXED && o.fp32_corrections;
+    ShiftedView sv64;
+    DevBuf x32, y32, scratch;
+    x32.st = y32.st = scratch.st = st;
+    if (corr32) {
+      if ((s = sv64.make(h, st))) return s;
+      DOCI_CUDA(cudaMallocAsync(&x32.p, sizeof(float) * D, st));
+      DOCI_CUDA(cudaMallocAsync(&y32.p, sizeof(float) * D, st));
+      DOCI_CUDA(cudaMallocAsync(&scratch.p, sizeof(double) * (2 * D + vec_partials_capacity() + 64), st));
+      op.ham32 = &sv64.view;
+      op.shift32 = sv64.shift;
+      op.x32 = static_cast<float *>(x32.p);
+      op.y32 = static_cast<float *>(y32.p);
+    }
+    int its64 = 0;
+    for (int round = 0;; ++round) {
+      op.anchor_next = true;
+      if ((s = davidson_run<double>(op, D, h->d_diag, static_cast<double *>(t.p), a, st, &out, d_x))) return s;
+      its64 += out.iterations;
+      if (!corr32) break;
+      // verification: one FP64 sigma of the result, its Rayleigh quotient and
+      // true residual (what the result reports)
+      double theta = 0, rnorm = 0;
+      double *d_y = static_cast<double *>(scratch.p), *d_r = d_y + D, *dp = d_r + D;
+      if ((s = fp64_check(op, d_x, D, d_y, d_r, dp, st, &theta, &rnorm))) return s;
+      ++its64;
+      out.energy = theta;
+      out.residual = rnorm;
+      out.converged = rnorm <= o.tol;
+      if (trace && trace_count && *trace_count < trace_len) {
+        double *r = trace + 4 * (*trace_count)++;
+        r[0] = 1;
+        r[1] = rnorm;
+        r[2] = theta;
+        r[3] = now_s() - trace_t0;
+      }
+      if (out.converged || round >= 2 || res->iterations_fp32 + its64 >= o.max_its) break;
+      a.max_its = o.max_its - res->iterations_fp32 - its64;
+      DOCI_CUDA(cudaMemcpyAsync(t.p, d_x, sizeof(double) * D, cudaMemcpyDeviceToDevice, st));
+    }
     res->energy = out.energy;
     res->residual = out.residual;
-    res->iterations = out.iterations + res->iterations_fp32;
+    res->iterations = its64 + res->iterations_fp32;
     res->converged = out.converged;
     res->status_code = out.return_code;
   } else if (o.solver == DOCI_SOLVER_CG || o.solver == DOCI_SOLVER_CGP) {

@@ -81,7 +81,16 @@ ShiftedView::~ShiftedView() {
 int MatvecOp::apply(const void *d_x, void *d_y, int precision, cudaStream_t st) {
   if (ham) {
     if (events_on) cudaEventRecord(ev0, st);
-    int s = launch_sigma(ham, d_x, d_y, precision, st);
+    int s;
+    if (ham32 && precision == DOCI_FP64 && !anchor_next) {
+      const double *x = static_cast<const double *>(d_x);
+      s = vec_convert<double, float>(x, x32, n, st);
+      if (s == DOCI_OK) s = launch_sigma(ham32, x32, y32, DOCI_FP32, st);
+      if (s == DOCI_OK) s = vec_unshift(y32, shift32, x, static_cast<double *>(d_y), n, st);
+    } else {
+      s = launch_sigma(ham, d_x, d_y, precision, st);
+    }
+    anchor_next = false;
     if (events_on) {
       cudaEventRecord(ev1, st);
       cudaEventSynchronize(ev1);
@@ -178,6 +187,26 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
   int stall = 0;
   double best = 1e300;
   double t_norm2 = 0, proj2 = 0;  // ||t||^2 and ||V^T t||^2 from the residual pass
+  // Mixed sigma precisions (FP64 phase with FP32 correction sigmas): werr[i]
+  // weighs the rounding error of VA_i (0 for the FP64 anchor).  The entry
+  // S[i][j] = v_i . H v_j is taken from the more accurate side, VA_i . v_j
+  // or v_i . VA_j: the anchor's cross terms then carry no FP32 error, which
+  // would otherwise enter the Ritz vector at full size.
+  const bool mixed_sigmas = op.ham32 != nullptr && sizeof(S) == 8;
+  std::vector<double> werr(maxv, 0.0);
+  auto column = [&](int j) -> int {
+    DOCI_TRY(vec_multidot<S>(Vp, D, j + 1, VAp + static_cast<size_t>(j) * D, D, dp, st));
+    DOCI_TRY(fetch(j + 1));
+    for (int i = 0; i <= j; ++i) Sm[j * maxv + i] = red[i];
+    bool other = false;
+    for (int i = 0; i < j; ++i) other = other || werr[i] < werr[j];
+    if (!other) return DOCI_OK;
+    std::vector<double> a(red.begin(), red.begin() + j + 1);
+    DOCI_TRY(vec_multidot<S>(VAp, D, j + 1, Vp + static_cast<size_t>(j) * D, D, dp, st));
+    DOCI_TRY(fetch(j + 1));
+    for (int i = 0; i < j; ++i) Sm[j * maxv + i] = werr[i] < werr[j] ? red[i] : a[i];
+    return DOCI_OK;
+  };
   while (res > a.tol && its++ < a.max_its) {
     // ---- new search vector: orthogonalise t against V, normalise (davidson.c:133-176)
     S *Vm = Vp + static_cast<size_t>(m) * D;
@@ -207,20 +236,21 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
     // ---- the one matvec of the iteration (davidson.c:76)
     DOCI_TRY(op.apply(Vm, VAp + static_cast<size_t>(m) * D, precision, st));
     // ---- subspace column S[m][i] = V_i . VA_m (davidson.c:178-193)
-    DOCI_TRY(vec_multidot<S>(Vp, D, m + 1, VAp + static_cast<size_t>(m) * D, D, dp, st));
-    DOCI_TRY(fetch(m + 1));
-    for (int i = 0; i <= m; ++i) Sm[m * maxv + i] = red[i];
+    werr[m] = mixed_sigmas && m > 0 ? 1.0 : 0.0;  // only the run's first sigma is FP64 (the anchor)
+    DOCI_TRY(column(m));
     ++m;
     jacobi_eig(m, Sm.data(), maxv, w.data(), Y.data());
     if (m == maxv) {  // ---- deflation (davidson.c:83-89, :229-255)
       DOCI_CUDA(cudaMemcpyAsync(d_Y, Y.data(), sizeof(double) * maxv * keep, cudaMemcpyHostToDevice, st));
       DOCI_TRY(vec_deflate<S>(Vp, D, maxv, keep, d_Y, maxv, D, st));
       DOCI_TRY(vec_deflate<S>(VAp, D, maxv, keep, d_Y, maxv, D, st));
-      for (int cc = 0; cc < keep; ++cc) {
-        DOCI_TRY(vec_multidot<S>(Vp, D, cc + 1, VAp + static_cast<size_t>(cc) * D, D, dp, st));
-        DOCI_TRY(fetch(cc + 1));
-        for (int i = 0; i <= cc; ++i) Sm[cc * maxv + i] = red[i];
+      if (mixed_sigmas) {  // error weight of a kept vector: sum_k |Y[k][c]| werr[k]
+        std::vector<double> wn(keep, 0.0);
+        for (int cc = 0; cc < keep; ++cc)
+          for (int k = 0; k < maxv; ++k) wn[cc] += std::fabs(Y[cc * maxv + k]) * werr[k];
+        for (int cc = 0; cc < keep; ++cc) werr[cc] = wn[cc];
       }
+      for (int cc = 0; cc < keep; ++cc) DOCI_TRY(column(cc));
       m = keep;
       jacobi_eig(m, Sm.data(), maxv, w.data(), Y.data());
     }

@@ -21,6 +21,15 @@ struct MatvecOp {
   double sigma_seconds = 0;
   bool events_on = false;
   cudaEvent_t ev0{}, ev1{};
+  // FP64 phase of the mixed mode: the first FP64 sigma after `anchor_next`
+  // is a true FP64 sigma (the anchor vector); the later ones (correction
+  // vectors, whose coefficients in the Ritz vector are of the size of the
+  // residual) run on the shifted FP32 view: y = sigma32((float)x) + shift x.
+  // Their FP32 rounding enters the Ritz vector scaled by those coefficients.
+  const doci_ham *ham32 = nullptr;
+  double shift32 = 0;
+  float *x32 = nullptr, *y32 = nullptr;  // D-element scratch, owned by the caller
+  bool anchor_next = true;
   int apply(const void *d_x, void *d_y, int precision, cudaStream_t st);
   // nv vectors x + v ldx -> y + v ldy (consecutive columns); the device sigma
   // shares its neighbour work over up to four vectors per launch

@@ -22,6 +22,8 @@ int vec_residual(const S *V, const S *VA, size_t ld, int m, const double *y, dou
                  size_t n, S *t, double *x, double *partials, cudaStream_t st, double diag_shift = 0.0);
 // index of the smallest element (first on ties), synchronous
 int vec_argmin(const double *d, size_t n, int64_t *idx, cudaStream_t st);
+// y[j] = y32[j] + shift x[j]: an FP32 sigma of H - shift back to H, in FP64
+int vec_unshift(const float *y32, double shift, const double *x, double *y, size_t n, cudaStream_t st);
 // out[j] = (float)(d[j] - shift): the FP32 diagonal of the shifted operator H - shift
 int vec_shifted_diag32(const double *d, double shift, float *out, size_t n, cudaStream_t st);
 template <typename S>

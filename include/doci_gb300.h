@@ -249,6 +249,11 @@ typedef struct doci_solve_opts {
   double mixed_tol;      /* residual at which the FP32 phase hands over (mixed) */
   int print_level;       /* 0 silent, 1 reference summary lines, 2 per-iteration table */
   uint64_t seed;         /* random start seed (hf_init == 0) */
+  int fp32_corrections;  /* mixed mode, FP64 phase: 1 (default) = the sigmas of the correction
+                            vectors in FP32 on the shifted operator, each run anchored by an
+                            FP64 sigma of its start vector and closed by an FP64 sigma of the
+                            result (its Rayleigh quotient and true residual are reported);
+                            0 = every FP64-phase sigma in FP64 */
 } doci_solve_opts;
 
 typedef struct doci_solve_result {
