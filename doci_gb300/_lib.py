@@ -217,7 +217,7 @@ class Hamiltonian:
 
     def set_sigma_kernel(self, kind) -> None:
         """0/'auto', 1/'gather', 2/'row' (row + column-panel passes), 3/'row1' (row pass only)."""
-        kind = {"auto": 0, "gather": 1, "row": 2, "row1": 3, "rowx": 4, "rowxc": 5, "pair": 6}.get(kind, kind)
+        kind = {"auto": 0, "gather": 1, "row": 2, "row1": 3, "rowx": 4, "rowxc": 5, "pair": 6, "pairsmem": 7}.get(kind, kind)
         _check(lib().doci_ham_set_sigma_kernel(self._h, int(kind)), "doci_ham_set_sigma_kernel")
 
     def diagonal(self) -> np.ndarray:

@@ -259,7 +259,7 @@ int doci_sigma_plan(const doci_ham *h, int precision, int *kind, int *launches) 
 }
 
 int doci_ham_set_sigma_kernel(doci_ham *h, int kind) {
-  if (!h || kind < 0 || kind > 6) return DOCI_ERR_INVALID;
+  if (!h || kind < 0 || kind > 7) return DOCI_ERR_INVALID;
   h->sigma_kernel = kind;
   return DOCI_OK;
 }

@@ -138,7 +138,7 @@ int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, si
 int kernel_blocks(const void *kernel, int threads, size_t dyn, int *blocks);
 // pair-form sigma (sigma_pair.cu), FP32 only
 bool pair_fits(const doci_ham *h);
-int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t s);
+int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t s, bool lean);
 int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &row_start);
 int launch_bitstrings(const doci_ham *h, int64_t first, int64_t count, uint32_t *out, cudaStream_t s);
 int launch_ranks(const doci_ham *h, const uint32_t *bits, int64_t count, int64_t *out, cudaStream_t s);

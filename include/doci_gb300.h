@@ -178,8 +178,9 @@ int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int
  * time), 5 kind 4 plus the column-panel pass, 6 the (N-1)-pair form (FP32
  * only: gather the L neighbours of every (N-1)-pair set, multiply by K on the
  * tensor cores, scatter-add; atomic adds, so the last bits vary between
- * runs; FP64 requests use the automatic choice).  2-6 fall back to 1 when
- * the handle has no row tiling.  For tests and tuning. */
+ * runs; FP64 requests use the automatic choice), 7 the pair form with the
+ * own row's sums in shared memory (slower; for comparison).  2-7 fall back
+ * to 1 when the handle has no row tiling.  For tests and tuning. */
 int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
 
 /* The path doci_sigma takes for this handle and precision: *kind as in

@@ -50,7 +50,7 @@ def test_golden_sigma_diag_bits(name, fcidump, dg):
         assert np.array_equal(ranks.cpu().numpy(), np.arange(h.D))
 
 
-@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair"])
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair", "pairsmem"])
 @pytest.mark.parametrize("L,N,seed", [(16, 8, 21), (18, 5, 22), (20, 10, 23), (12, 1, 24), (12, 11, 25),
                                       (7, 0, 26), (6, 6, 27), (32, 2, 28), (32, 30, 29), (24, 12, 30),
                                       (22, 11, 31), (26, 4, 32)])
@@ -91,7 +91,7 @@ def test_addressing_full_size_properties(synth, dg):
             assert all(bin(int(v)).count("1") == 16 for v in b[:64])
 
 
-@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair"])
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair", "pairsmem"])
 def test_sigma_full_size_symmetry_and_linearity(kernel, synth, dg):
     """L=28, N=14 (D = 40,116,600): H is symmetric, sigma is linear, and
     sampled rows agree with the oracle's gather form."""
@@ -126,7 +126,7 @@ def test_sigma_full_size_symmetry_and_linearity(kernel, synth, dg):
         assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair"])
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair", "pairsmem"])
 def test_sigma_L32_fp32_vs_oracle_samples(kernel, synth, dg):
     """L=32, N=16 (D = 601,080,390), FP32: sampled rank windows across the
     whole space (start, middle, end) against the FP64 oracle gather form."""
