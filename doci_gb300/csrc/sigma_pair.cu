@@ -100,6 +100,10 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, tq = lane & 3;
   float(*tile)[kTileStride] = sm.tile[warp];
+  {
+    float4 *tz = reinterpret_cast<float4 *>(&tile[0][0]);
+    for (int z = lane; z < 32 * kTileStride / 4; z += 32) tz[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
 
   for (int blk = blockIdx.x; blk < s.nblocks; blk += gridDim.x) {
     const uint2 bw = blocks[blk];
@@ -141,9 +145,12 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
       const uint32_t c = s0 + threadIdx.x;
       const bool live = c < n_s;
       {
+        // X_S is zero on the column orbitals in S: clear the column-part rows
+        // (the row-part rows are written for every live set; rows past the
+        // block's orbitals meet zero K rows and only need to be finite, which
+        // the clear at kernel start and the later Y values are)
         float4 *tz = reinterpret_cast<float4 *>(&tile[0][0]);
-#pragma unroll
-        for (int z = lane; z < 32 * kTileStride / 4; z += 32) tz[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int z = lane; z < sp * (kTileStride / 4); z += 32) tz[z] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
       __syncwarp();
       // gather X_S: column holes of C' (row R', positions from the insertion
