@@ -90,6 +90,17 @@ int make_start(doci_ham *h, int hf_init, uint64_t seed, double *d_t, cudaStream_
   return vec_fill_random(d_t, h->D, seed, st);
 }
 
+// Device address of a pinned (page-locked, mapped) host buffer, or null for
+// pageable memory.
+const void *mapped_host(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // pageable memory on older drivers reports an error
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // One FP64 sigma y = H x (through op, as an anchor), theta = x.y / x.x and
 // the residual norm ||y - theta x|| / ||x||.  dp: partial-sum scratch of
 // vec_partials_capacity() + 64 doubles; r: D doubles of scratch.
@@ -270,10 +281,23 @@ int doci_sigma_host(doci_ham *h, const void *x, void *y, int precision) {
   const size_t bytes = static_cast<size_t>(h->D) * (precision == DOCI_FP64 ? 8 : 4);
   int st = ham_stage(h, bytes);
   if (st) return st;
-  DOCI_CUDA(cudaMemcpyAsync(h->d_stage_x, x, bytes, cudaMemcpyHostToDevice, h->stream));
+  // pinned host buffers are read and written by copy kernels through their
+  // device mapping (all SMs on the host link, faster than one copy engine);
+  // pageable ones go through cudaMemcpyAsync
+  const void *dx = mapped_host(x);
+  void *dy = const_cast<void *>(mapped_host(y));
+  if (dx) {
+    if ((st = vec_copy(h->d_stage_x, dx, bytes, h->stream))) return st;
+  } else {
+    DOCI_CUDA(cudaMemcpyAsync(h->d_stage_x, x, bytes, cudaMemcpyHostToDevice, h->stream));
+  }
   st = launch_sigma(h, h->d_stage_x, h->d_stage_y, precision, h->stream);
   if (st) return st;
-  DOCI_CUDA(cudaMemcpyAsync(y, h->d_stage_y, bytes, cudaMemcpyDeviceToHost, h->stream));
+  if (dy) {
+    if ((st = vec_copy(dy, h->d_stage_y, bytes, h->stream))) return st;
+  } else {
+    DOCI_CUDA(cudaMemcpyAsync(y, h->d_stage_y, bytes, cudaMemcpyDeviceToHost, h->stream));
+  }
   DOCI_CUDA(cudaStreamSynchronize(h->stream));
   return DOCI_OK;
 }

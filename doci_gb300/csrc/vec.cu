@@ -677,6 +677,31 @@ __global__ void unshift_kernel(const float *__restrict__ y32, double shift, cons
 }
 }  // namespace
 
+namespace {
+__global__ void copy16_kernel(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    dst[j] = src[j];
+}
+__global__ void copy4_kernel(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    dst[j] = src[j];
+}
+}  // namespace
+
+int vec_copy(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src);
+  if ((a % 16) == 0 && (bytes % 16) == 0)
+    copy16_kernel<<<grid_blocks() * 2, kT, 0, st>>>(static_cast<const uint4 *>(src), static_cast<uint4 *>(dst),
+                                                    bytes / 16);
+  else if ((a % 4) == 0 && (bytes % 4) == 0)
+    copy4_kernel<<<grid_blocks() * 2, kT, 0, st>>>(static_cast<const uint32_t *>(src), static_cast<uint32_t *>(dst),
+                                                   bytes / 4);
+  else
+    return DOCI_ERR_INVALID;
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
 int vec_unshift(const float *y32, double shift, const double *x, double *y, size_t n, cudaStream_t st) {
   unshift_kernel<<<grid_blocks(), kT, 0, st>>>(y32, shift, x, y, n);
   DOCI_CUDA(cudaGetLastError());

@@ -22,6 +22,9 @@ int vec_residual(const S *V, const S *VA, size_t ld, int m, const double *y, dou
                  size_t n, S *t, double *x, double *partials, cudaStream_t st, double diag_shift = 0.0);
 // index of the smallest element (first on ties), synchronous
 int vec_argmin(const double *d, size_t n, int64_t *idx, cudaStream_t st);
+// bytes from src to dst by a kernel (both device-accessible: device memory or
+// pinned host memory mapped into the device's address space)
+int vec_copy(void *dst, const void *src, size_t bytes, cudaStream_t st);
 // y[j] = y32[j] + shift x[j]: an FP32 sigma of H - shift back to H, in FP64
 int vec_unshift(const float *y32, double shift, const double *x, double *y, size_t n, cudaStream_t st);
 // out[j] = (float)(d[j] - shift): the FP32 diagonal of the shifted operator H - shift

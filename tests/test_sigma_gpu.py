@@ -226,3 +226,34 @@ def test_sigma_plan(synth, dg):
     with dg.Hamiltonian.from_fcidump(synth(12, 6, 52)) as h:
         assert h.sigma_plan(dg.FP32) == (1, 1)
         assert h.sigma_plan(dg.FP64) == (1, 1)
+
+
+@pytest.mark.parametrize("prec_name", ["FP64", "FP32"])
+def test_sigma_host_pinned_and_pageable(prec_name, synth, dg):
+    """doci_sigma_host on pinned host buffers (copied by kernels through
+    their device mapping), on pageable ones (cudaMemcpyAsync), and on an
+    offset inside a pinned buffer: all equal doci_sigma on device buffers."""
+    torch = torch_cuda()
+    import ctypes as C
+    prec = getattr(dg, prec_name)
+    tdt = torch.float64 if prec == dg.FP64 else torch.float32
+    with dg.Hamiltonian.from_fcidump(synth(18, 9, 61)) as h:
+        h.set_sigma_kernel("row1")  # deterministic: results compare bit for bit
+        D = h.D
+        x = torch.randn(D + 7, dtype=tdt, generator=torch.Generator().manual_seed(3))
+        xd = x[:D].cuda()
+        yd = torch.empty_like(xd)
+        h.sigma_device(xd.data_ptr(), yd.data_ptr(), prec)
+        torch.cuda.synchronize()
+        ref = yd.cpu()
+        lib = dg.lib()
+        for pinned, off in ((True, 0), (True, 3), (False, 0)):
+            xs = x.pin_memory() if pinned else x.clone()
+            ys = torch.full((D + 7,), float("nan"), dtype=tdt)
+            ys = ys.pin_memory() if pinned else ys
+            src = xs[off:off + D] if off else xs[:D]
+            if off:  # same values at an offset inside the buffer
+                src.copy_(x[:D])
+            st = lib.doci_sigma_host(h.handle, C.c_void_p(src.data_ptr()), C.c_void_p(ys[off:].data_ptr()), prec)
+            assert st == 0
+            assert torch.equal(ys[off:off + D], ref), (pinned, off)
