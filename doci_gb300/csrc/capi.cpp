@@ -319,6 +319,7 @@ int doci_multidot(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   double *partials = nullptr;
   DOCI_CUDA(cudaMallocAsync(&partials, sizeof(double) * vec_partials_capacity(), st));
+  if (const int si = vec_partials_init(partials, st)) return si;
   int s = precision == DOCI_FP64
               ? vec_multidot<double>(static_cast<const double *>(d_V), static_cast<size_t>(ld), m,
                                      static_cast<const double *>(d_w), static_cast<size_t>(n), partials, st)
@@ -464,6 +465,7 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
       DOCI_CUDA(cudaMallocAsync(&x32.p, sizeof(float) * D, st));
       DOCI_CUDA(cudaMallocAsync(&y32.p, sizeof(float) * D, st));
       DOCI_CUDA(cudaMallocAsync(&scratch.p, sizeof(double) * (2 * D + vec_partials_capacity() + 64), st));
+      if ((s = vec_partials_init(static_cast<double *>(scratch.p) + 2 * D, st))) return s;
       op.ham32 = &sv64.view;
       op.shift32 = sv64.shift;
       op.x32 = static_cast<float *>(x32.p);

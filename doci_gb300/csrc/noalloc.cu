@@ -62,8 +62,10 @@ extern "C" int doci_multidot_noalloc(const void *d_V, int64_t ld, int m, const v
   if (!d_V || !d_w || !d_out || m < 1 || n < 0 || ld < n) return DOCI_ERR_INVALID;
   if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
   if (m > kMaxM) return DOCI_ERR_SCRATCH_LIMIT;
-  // the reduction launches vec_reduction_blocks() blocks, each writing m partials
-  if (vec_reduction_blocks() > kMaxBlocks) return DOCI_ERR_SCRATCH_LIMIT;
+  // the partial-sum buffer the projection pass needs: a counter and the
+  // results (36 doubles; the counter starts at zero with the array and every
+  // pass resets it) and m partials per block
+  if (36 + static_cast<int64_t>(vec_reduction_blocks()) * m > kScratchDoubles) return DOCI_ERR_SCRATCH_LIMIT;
   double *scratch = nullptr;
   const int s0 = scratch_address(&scratch);
   if (s0 != DOCI_OK) return s0;

@@ -166,6 +166,7 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
   DOCI_TRY(V.alloc(sizeof(S) * D * maxv, st));
   DOCI_TRY(VA.alloc(sizeof(S) * D * maxv, st));
   DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity(), st));
+  DOCI_TRY(vec_partials_init(part.as<double>(), st));
   // small device scratch: [0,64) reduction output, [64,96) y/c, [96, 96+32*32) Y
   DOCI_TRY(small.alloc(sizeof(double) * (96 + 32 * 32), st));
   double *d_red = small.as<double>(), *d_vec = d_red + 64, *d_Y = d_red + 96;
@@ -174,8 +175,7 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
   std::vector<double> Sm(maxv * maxv, 0.0), Y(maxv * maxv, 0.0), w(maxv, 0.0), red(64), c(32, 0.0);
 
   auto fetch = [&](int nk) -> int {
-    DOCI_TRY(vec_reduce(dp, nk, d_red, st));
-    DOCI_CUDA(cudaMemcpyAsync(red.data(), d_red, sizeof(double) * nk, cudaMemcpyDeviceToHost, st));
+    DOCI_CUDA(cudaMemcpyAsync(red.data(), vec_results(dp), sizeof(double) * nk, cudaMemcpyDeviceToHost, st));
     DOCI_CUDA(cudaStreamSynchronize(st));
     return DOCI_OK;
   };
@@ -342,14 +342,14 @@ int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, con
   DOCI_TRY(VA.alloc(sizeof(S) * D * maxv, st));
   DOCI_TRY(tbuf.alloc(sizeof(S) * D * R, st));
   DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity(), st));
+  DOCI_TRY(vec_partials_init(part.as<double>(), st));
   DOCI_TRY(small.alloc(sizeof(double) * (96 + 32 * 32), st));
   double *d_red = small.as<double>(), *d_vec = d_red + 64, *d_Y = d_red + 96;
   S *Vp = V.as<S>(), *VAp = VA.as<S>(), *Tp = tbuf.as<S>();
   double *dp = part.as<double>();
   std::vector<double> Sm(maxv * maxv, 0.0), Y(maxv * maxv, 0.0), w(maxv, 0.0), red(64);
   auto fetch = [&](int nk) -> int {
-    DOCI_TRY(vec_reduce(dp, nk, d_red, st));
-    DOCI_CUDA(cudaMemcpyAsync(red.data(), d_red, sizeof(double) * nk, cudaMemcpyDeviceToHost, st));
+    DOCI_CUDA(cudaMemcpyAsync(red.data(), vec_results(dp), sizeof(double) * nk, cudaMemcpyDeviceToHost, st));
     DOCI_CUDA(cudaStreamSynchronize(st));
     return DOCI_OK;
   };
@@ -486,13 +486,13 @@ int ray_q_run(MatvecOp &op, size_t D, const double *d_diag_or_null, double *d_x,
   DevMem buf, part, small;
   DOCI_TRY(buf.alloc(sizeof(double) * D * 5, st));
   DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity(), st));
+  DOCI_TRY(vec_partials_init(part.as<double>(), st));
   DOCI_TRY(small.alloc(sizeof(double) * 64, st));
   double *p = buf.as<double>(), *Ax = p + D, *Ap = Ax + D, *g = Ap + D, *pinv = g + D;
   double *dp = part.as<double>(), *d_red = small.as<double>();
   double red[8];
   auto fetch = [&](int nk) -> int {
-    DOCI_TRY(vec_reduce(dp, nk, d_red, st));
-    DOCI_CUDA(cudaMemcpyAsync(red, d_red, sizeof(double) * nk, cudaMemcpyDeviceToHost, st));
+    DOCI_CUDA(cudaMemcpyAsync(red, vec_results(dp), sizeof(double) * nk, cudaMemcpyDeviceToHost, st));
     DOCI_CUDA(cudaStreamSynchronize(st));
     return DOCI_OK;
   };

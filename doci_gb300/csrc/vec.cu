@@ -34,10 +34,20 @@ constexpr int kMaxK = 34;  // outputs of one reduction pass
 
 int grid_blocks() { return device_sm_count() * 4; }
 
+// Partial-sum buffer layout: [0] a block counter, [1, 1 + kMaxK) the
+// results, then one row of nk partials per block.  Every reduction pass ends
+// with block_reduce_store: each block writes its row, and the last block to
+// finish (the counter) sums the rows in a fixed order (one warp per output,
+// lanes over strided blocks, then a fixed shuffle tree) into the results and
+// resets the counter -- results do not depend on timing, and no separate
+// reduction launch is needed.
+constexpr int kHeader = 1 + kMaxK;
+
 template <int K>
 __device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, double *partials) {
-  __shared__ double red[kT / 32][kMaxK];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ double red[32][kMaxK];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     if (k < nk) {
@@ -48,29 +58,27 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, dou
     }
   }
   __syncthreads();
+  double *rows = partials + kHeader;
   if (threadIdx.x < nk) {
     double s = 0;
-    for (int w = 0; w < kT / 32; ++w) s += red[w][threadIdx.x];
-    partials[static_cast<size_t>(blockIdx.x) * nk + threadIdx.x] = s;
+    for (int w = 0; w < nw; ++w) s += red[w][threadIdx.x];
+    rows[static_cast<size_t>(blockIdx.x) * nk + threadIdx.x] = s;
   }
-}
-
-// out[k] = sum_b partials[b][k]; fixed order
-__global__ void reduce_partials_kernel(const double *__restrict__ partials, int nblocks, int nk,
-                                       double *__restrict__ out) {
-  __shared__ double red[kT];
-  for (int k = 0; k < nk; ++k) {
+  __threadfence();
+  __syncthreads();
+  unsigned int *counter = reinterpret_cast<unsigned int *>(partials);
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int k = warp; k < nk; k += nw) {
     double s = 0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[static_cast<size_t>(b) * nk + k];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) out[k] = red[0];
-    __syncthreads();
+    for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(rows + static_cast<size_t>(b) * nk + k);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) partials[1 + k] = s;
   }
+  if (threadIdx.x == 0) *counter = 0u;
 }
 
 // partials of V_i . w for i < m
@@ -229,51 +237,38 @@ combine_kernel(const S *__restrict__ V, size_t ld, int m, const double *__restri
 constexpr int kChunk = 16;
 
 // Per-thread FP64 accumulators kept in shared memory ([k][thread], so the
-// registers hold only the FP32 chunk sums); flushed once per chunk.  Up to 18
-// accumulators (37 KB per block; static shared memory stops at 48 KB); more
-// stay in registers (RegAcc).
-template <int NK>
-struct RegAcc {
-  double a[NK];
-  __device__ __forceinline__ void zero() {
-#pragma unroll
-    for (int k = 0; k < NK; ++k) a[k] = 0;
-  }
-  __device__ __forceinline__ void add(const float (&f)[NK], int nk) {
-#pragma unroll
-    for (int k = 0; k < NK; ++k)
-      if (k < nk) a[k] += f[k];
-  }
-  __device__ __forceinline__ void store(int nk, double *partials) { block_reduce_store<NK>(a, nk, partials); }
-};
+// registers hold only the FP32 chunk sums); flushed once per chunk.  Blocks
+// of BT threads: 256 for up to 16 basis vectors, 128 for up to 32 (18 or 34
+// accumulators: 37 / 35 KB of static shared memory).
+template <int K>
+__host__ __device__ constexpr int f32_block() { return K <= 16 ? 256 : 128; }
 
-template <int NK>
+template <int NK, int BT>
 struct SmemAcc {
   double *a;
   __device__ __forceinline__ void zero() {
 #pragma unroll
-    for (int k = 0; k < NK; ++k) a[k * kT + threadIdx.x] = 0;
+    for (int k = 0; k < NK; ++k) a[k * BT + threadIdx.x] = 0;
   }
   __device__ __forceinline__ void add(const float (&f)[NK], int nk) {
 #pragma unroll
     for (int k = 0; k < NK; ++k)
-      if (k < nk) a[k * kT + threadIdx.x] += f[k];
+      if (k < nk) a[k * BT + threadIdx.x] += f[k];
   }
   __device__ __forceinline__ void store(int nk, double *partials) {
     double acc[NK];
 #pragma unroll
-    for (int k = 0; k < NK; ++k) acc[k] = k < nk ? a[k * kT + threadIdx.x] : 0.0;
+    for (int k = 0; k < NK; ++k) acc[k] = k < nk ? a[k * BT + threadIdx.x] : 0.0;
     block_reduce_store<NK>(acc, nk, partials);
   }
 };
 
 template <int K>
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(f32_block<K>())
 multidot_f32_kernel(const float *__restrict__ V, size_t ld, int m, const float *__restrict__ w, size_t n,
                     double *__restrict__ partials) {
-  __shared__ double acc_s[(K <= 16 ? K : 1) * kT];
-  typename std::conditional<K <= 16, SmemAcc<K>, RegAcc<K>>::type acc{};
-  if constexpr (K <= 16) acc.a = acc_s;
+  __shared__ double acc_s[K * f32_block<K>()];
+  SmemAcc<K, f32_block<K>()> acc{acc_s};
   acc.zero();
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t j0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j0 < n; j0 += stride * kChunk) {
@@ -295,15 +290,14 @@ multidot_f32_kernel(const float *__restrict__ V, size_t ld, int m, const float *
 }
 
 template <int K>
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(f32_block<K>())
 residual_f32_kernel(const float *__restrict__ V, const float *__restrict__ VA, size_t ld, int m,
                     const double *__restrict__ y, double theta, double pre_theta, const double *__restrict__ diag,
                     size_t n, float *__restrict__ t, double *__restrict__ x_out, double *__restrict__ partials) {
   __shared__ float ys[K];
-  __shared__ double acc_s[(K <= 16 ? K + 2 : 1) * kT];
+  __shared__ double acc_s[(K + 2) * f32_block<K>()];
   if (threadIdx.x < K) ys[threadIdx.x] = threadIdx.x < m ? static_cast<float>(y[threadIdx.x]) : 0.f;
-  typename std::conditional<K <= 16, SmemAcc<K + 2>, RegAcc<K + 2>>::type acc{};
-  if constexpr (K <= 16) acc.a = acc_s;
+  SmemAcc<K + 2, f32_block<K>()> acc{acc_s};
   acc.zero();
   __syncthreads();
   const float th = static_cast<float>(theta);
@@ -341,14 +335,13 @@ residual_f32_kernel(const float *__restrict__ V, const float *__restrict__ VA, s
 }
 
 template <int K>
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(f32_block<K>())
 gs_update_f32_kernel(const float *__restrict__ V, size_t ld, int m, const double *__restrict__ c, size_t n,
                      float *__restrict__ t, double *__restrict__ partials) {
   __shared__ float cs[K];
-  __shared__ double acc_s[(K <= 16 ? K + 1 : 1) * kT];
+  __shared__ double acc_s[(K + 1) * f32_block<K>()];
   if (threadIdx.x < K) cs[threadIdx.x] = threadIdx.x < m ? static_cast<float>(c[threadIdx.x]) : 0.f;
-  typename std::conditional<K <= 16, SmemAcc<K + 1>, RegAcc<K + 1>>::type acc{};
-  if constexpr (K <= 16) acc.a = acc_s;
+  SmemAcc<K + 1, f32_block<K>()> acc{acc_s};
   acc.zero();
   __syncthreads();
   const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -597,7 +590,7 @@ template <typename S, int K>
 struct MultidotL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const S *w, size_t n, double *p) {
     if constexpr (std::is_same<S, float>::value)
-      multidot_f32_kernel<K><<<g, kT, 0, st>>>(V, ld, m, w, n, p);
+      multidot_f32_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, ld, m, w, n, p);
     else
       multidot_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, w, n, p);
   }
@@ -613,7 +606,8 @@ struct ResidualL {
   static void run(int g, cudaStream_t st, const S *V, const S *VA, size_t ld, int m, const double *y, double th,
                   double pre, const double *diag, size_t n, S *t, double *x, double *p) {
     if constexpr (std::is_same<S, float>::value)
-      residual_f32_kernel<K><<<g, kT, 0, st>>>(V, VA, ld, m, y, th, pre, diag, n, t, x, p);
+      residual_f32_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, VA, ld, m, y, th, pre, diag, n,
+                                                                              t, x, p);
     else
       residual_kernel<S, K><<<g, kT, 0, st>>>(V, VA, ld, m, y, th, pre, diag, n, t, x, p);
   }
@@ -622,7 +616,7 @@ template <typename S, int K>
 struct GsUpdateL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *p) {
     if constexpr (std::is_same<S, float>::value)
-      gs_update_f32_kernel<K><<<g, kT, 0, st>>>(V, ld, m, c, n, t, p);
+      gs_update_f32_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, ld, m, c, n, t, p);
     else
       gs_update_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, c, n, t, p);
   }
@@ -658,7 +652,15 @@ struct CombineL {
 
 }  // namespace
 
-int vec_partials_capacity() { return grid_blocks() * kMaxK; }
+// the largest grid a reduction pass launches is 2 grid_blocks()
+int vec_partials_capacity() { return kHeader + 2 * grid_blocks() * kMaxK; }
+
+int vec_partials_init(double *partials, cudaStream_t st) {
+  DOCI_CUDA(cudaMemsetAsync(partials, 0, sizeof(double), st));
+  return DOCI_OK;
+}
+
+const double *vec_results(const double *partials) { return partials + 1; }
 
 int vec_reduction_blocks() { return grid_blocks(); }
 
@@ -715,8 +717,8 @@ int vec_shifted_diag32(const double *d, double shift, float *out, size_t n, cuda
 }
 
 int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st) {
-  reduce_partials_kernel<<<1, kT, 0, st>>>(partials, grid_blocks(), nk, out);
-  DOCI_CUDA(cudaGetLastError());
+  // the pass itself reduced its partials; copy its results
+  DOCI_CUDA(cudaMemcpyAsync(out, partials + 1, sizeof(double) * nk, cudaMemcpyDeviceToDevice, st));
   return DOCI_OK;
 }
 

@@ -7,11 +7,17 @@
 
 namespace doci {
 
-// partial-sum buffer size (doubles) the reductions below need
+// Partial-sum buffer of the reductions below (doubles): a block counter, the
+// results, one row per block.  Every reduction pass finishes its own sum (in
+// a fixed order) into the results; initialise a new buffer's counter once
+// with vec_partials_init.
 int vec_partials_capacity();
-// number of blocks (rows of partial sums) every reduction kernel launches
+int vec_partials_init(double *partials, cudaStream_t st);
+// the results of the last reduction pass on `partials` (device pointer)
+const double *vec_results(const double *partials);
+// the default number of blocks of a reduction pass (the largest is twice it)
 int vec_reduction_blocks();
-// out[k] = sum over blocks of partials[b][k], k < nk (device, fixed order)
+// out[k] = result k of the last pass, k < nk (device to device copy)
 int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st);
 
 template <typename S>
