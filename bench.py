@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge measurement")
+    ap.add_argument("--converge-repeats", type=int, default=20,
+                    help="mixed solves of the L=28 N=14 Hamiltonian for time-to-converge p50/p99 (0 = none)")
     ap.add_argument("--workload", choices=["sigma", "batch", "serve", "solve"], default="sigma",
                     help="sigma: the headline sigma benchmark; batch: many Hamiltonians, several roots; "
                          "serve: Poisson request stream through the request server")
@@ -213,6 +215,32 @@ def converge_report(h, max_vec: int, mixed_tol: float, threshold: float = 1e-8):
             "mixed_iterations_fp64": rmx["iterations"] - rmx["iterations_fp32"],
             "fp64_residual_final": r64["residual"], "max_vec": max_vec, "mixed_tol": mixed_tol,
             "note": "wall time from a built Hamiltonian (integrals, tables, diagonal on the device)"}
+
+
+def converge_repeats(L: int, N: int, seed: int, repeats: int, max_vec: int, mixed_tol: float,
+                     threshold: float = 1e-8):
+    """p50/p99 of the time to |E - E_FP64| < threshold over `repeats` mixed
+    solves of one Hamiltonian (the FP32 pair-form sigma adds with atomics, so
+    repeats differ in their last bits and timings), E_FP64 from one FP64
+    solve of the same Hamiltonian."""
+    import numpy as np
+    import doci_gb300 as dg
+    common = dict(solver="D", davidson_max_vec=max_vec, davidson_keep=2, max_its=300)
+    with dg.Hamiltonian.from_fcidump(workload_path(L, N, seed, 0, 1)) as h:
+        r64, _, t64 = h.solve_trace(tol=1e-7, mode="fp64", **common)
+        e_ref = r64["energy"]
+        hit64 = next((float(t) for ph, _, e, t in t64 if abs(e - e_ref) < threshold), None)
+        times, dEs = [], []
+        for _ in range(repeats):
+            rmx, _, tmx = h.solve_trace(tol=1e-7, mode="mixed", mixed_tol=mixed_tol, **common)
+            hit = next((float(t) for ph, _, e, t in tmx if ph == 1 and abs(e - e_ref) < threshold), None)
+            if hit is not None:
+                times.append(hit)
+            dEs.append(abs(rmx["energy"] - e_ref))
+    return {"workload": f"L={L} N={N} seed={seed}", "repeats": repeats, "reached": len(times),
+            "fp64_s": hit64, "mixed_p50_s": pct(times, 50), "mixed_p99_s": pct(times, 99),
+            "mixed_max_s": max(times) if times else None, "dE_final_max": max(dEs) if dEs else None,
+            "max_vec": max_vec, "mixed_tol": mixed_tol}
 
 
 def cpu_sample(path: str, seconds: float, seed: int = 0):
@@ -467,6 +495,8 @@ def main():
         del x, y
         torch.cuda.empty_cache()
         conv = converge_report(h, a.max_vec, a.mixed_tol)
+        if a.converge_repeats > 0:
+            conv["repeats_L28"] = converge_repeats(28, 14, 2, a.converge_repeats, a.max_vec, a.mixed_tol)
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         s = cpu_sample(path, a.cpu_seconds)
