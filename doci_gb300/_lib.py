@@ -106,6 +106,7 @@ def lib() -> C.CDLL:
         "doci_sigma": (i, [vp, vp, vp, i, vp]),
         "doci_sigma_block": (i, [vp, vp, C.c_int64, vp, C.c_int64, i, i, vp]),
         "doci_sigma_plan": (i, [vp, i, C.POINTER(i), C.POINTER(i)]),
+        "doci_ham_autotune": (i, [vp, i, i, C.POINTER(i)]),
         "doci_sigma_host": (i, [vp, vp, vp, i]),
         "doci_ham_set_sigma_kernel": (i, [vp, i]),
         "doci_bitstrings": (i, [vp, i64, i64, vp, vp]),
@@ -242,6 +243,12 @@ class Hamiltonian:
         """sigma on device buffers (e.g. torch tensors' data_ptr())."""
         _check(lib().doci_sigma(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), precision,
                                 C.c_void_p(stream or None)), "doci_sigma")
+
+    def autotune(self, precision: int = FP32, nvec: int = 1) -> int:
+        """Time the sigma paths for this shape and keep the fastest (process-wide)."""
+        c = C.c_int()
+        _check(lib().doci_ham_autotune(self._h, precision, nvec, C.byref(c)), "doci_ham_autotune")
+        return c.value
 
     def sigma_plan(self, precision: int = FP64):
         """(kind, launches) of doci_sigma on this handle: the kernel the

@@ -269,6 +269,11 @@ int doci_sigma_plan(const doci_ham *h, int precision, int *kind, int *launches) 
   return DOCI_OK;
 }
 
+int doci_ham_autotune(doci_ham *h, int precision, int nvec, int *choice) {
+  if (!h || nvec < 1 || nvec > 4) return DOCI_ERR_INVALID;
+  return autotune_sigma(h, precision, nvec, h->stream, choice);
+}
+
 int doci_ham_set_sigma_kernel(doci_ham *h, int kind) {
   if (!h || kind < 0 || kind > 7) return DOCI_ERR_INVALID;
   h->sigma_kernel = kind;

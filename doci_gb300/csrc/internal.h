@@ -126,6 +126,12 @@ struct SigmaPlan {
   int kind, launches;
 };
 SigmaPlan plan_sigma(const doci_ham *h, int precision, bool allow_pair = true);
+// Time the sigma paths that fit this handle's shape (nv = 1: single sigma,
+// with and without the pair form; 2..4: the block paths) and keep the
+// fastest for every handle of the same (device, L, N, precision) in this
+// process; *choice gets the pick (a kind for nv = 1, a block method else).
+int autotune_sigma(doci_ham *h, int precision, int nv, cudaStream_t s, int *choice);
+bool sigma_tuned(const doci_ham *h, int precision, int nv);
 // allow_pair = false keeps the FP32 result run-to-run reproducible (the pair
 // form adds with atomics)
 int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t s, bool allow_pair = true);

@@ -12,6 +12,7 @@
 
 #include <mutex>
 #include <map>
+#include <tuple>
 #include <set>
 #include <type_traits>
 #include <vector>
@@ -881,30 +882,67 @@ unsigned grid_for(uint64_t n) {
 
 }  // namespace
 
-SigmaPlan plan_sigma(const doci_ham *h, int precision, bool allow_pair) {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Autotuning: the kernel path per problem shape, chosen by timing the
+// candidates (doci_ham_autotune).  Choices are kept per (device, L, N,
+// precision, vectors, pair form allowed) for the whole process: the kernels'
+// speed depends on the shape, not on the integrals.
+// ---------------------------------------------------------------------------
+struct TuneKey {
+  int device, L, N, precision, nv, allow_pair;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(device, L, N, precision, nv, allow_pair) <
+           std::tie(o.device, o.L, o.N, o.precision, o.nv, o.allow_pair);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tuned;
+
+TuneKey tune_key(const doci_ham *h, int precision, int nv, bool allow_pair) {
+  return TuneKey{h->device, h->L, h->N, precision, nv, allow_pair ? 1 : 0};
+}
+
+int tuned_choice(const doci_ham *h, int precision, int nv, bool allow_pair) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(tune_key(h, precision, nv, allow_pair));
+  return it == g_tuned.end() ? 0 : it->second;
+}
+
+// The path of kind `kind` (0 = the heuristics) for this handle; a kind that
+// does not fit falls back as described at doci_ham_set_sigma_kernel.
+SigmaPlan plan_kind(const doci_ham *h, int precision, bool allow_pair, int kind) {
   const size_t elem = precision == DOCI_FP64 ? 8 : 4;
   // pair form: on request (kind 6), and the automatic FP32 choice when its
   // blocks give every SM work (measured fastest there); FP32 only
-  const bool want_pair =
-      h->sigma_kernel == 6 || h->sigma_kernel == 7 || (h->sigma_kernel == 0 && h->npblocks >= device_sm_count());
+  const bool want_pair = kind == 6 || kind == 7 || (kind == 0 && h->npblocks >= device_sm_count());
   if (allow_pair && want_pair && precision == DOCI_FP32 && pair_fits(h))
-    return {h->sigma_kernel == 7 ? 7 : 6, 2};  // init pass + pair pass
+    return {kind == 7 ? 7 : 6, 2};  // init pass + pair pass
   // row kernel when the row tiling exists, fits, and gives every SM work
-  bool row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
+  bool row = kind >= 2 || (kind == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
   if (!row) return {1, 1};
   // automatic: the phase-ordered pass for FP64 (measured faster there), the
   // single row pass for FP32 (measured faster there)
-  const bool want_rowx = h->sigma_kernel >= 4 || (h->sigma_kernel == 0 && precision == DOCI_FP64);
+  const bool want_rowx = kind >= 4 || (kind == 0 && precision == DOCI_FP64);
   if (want_rowx && rowx_fits(h, elem)) {
     // kind 5 moves the row-part hops to the column-panel pass
-    const bool colp = h->sigma_kernel == 5 && col_pass_fits(h, elem);
+    const bool colp = kind == 5 && col_pass_fits(h, elem);
     return colp ? SigmaPlan{5, 2} : SigmaPlan{4, 1};
   }
   // row-part hops in the column-panel pass only on request (kind 2): the
   // single row pass (kind 3, and the automatic choice) measured faster
-  const bool col = h->sigma_kernel == 2 && col_pass_fits(h, elem);
+  const bool col = kind == 2 && col_pass_fits(h, elem);
   return col ? SigmaPlan{2, 2} : SigmaPlan{3, 1};
+}
+
+}  // namespace
+
+SigmaPlan plan_sigma(const doci_ham *h, int precision, bool allow_pair) {
+  int kind = h->sigma_kernel;
+  if (kind == 0) kind = tuned_choice(h, precision, 1, allow_pair);  // a tuned shape: its measured best
+  return plan_kind(h, precision, allow_pair, kind);
 }
 
 int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t st, bool allow_pair) {
@@ -931,24 +969,36 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
   return f64 ? launch_col<double>(h, x, y, st) : launch_col<float>(h, x, y, st);
 }
 
-int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv, int precision,
-                       cudaStream_t st) {
-  if (nv < 1 || nv > 4 || ldx < h->D || ldy < h->D) return DOCI_ERR_INVALID;
-  if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
-  const size_t elem = precision == DOCI_FP64 ? 8 : 4;
-  // the block solves stay run-to-run reproducible: no pair form here
-  if (nv == 1) return launch_sigma(h, x, y, precision, st, false);
-  const char *xc = static_cast<const char *>(x);
-  char *yc = static_cast<char *>(y);
-  // row pass: every vector's row staged in shared memory, so the group size
-  // is what fits beside the static tables (at most 212 KB of rows)
+namespace {
+
+// multi-vector methods
+constexpr int kMultiRow = 1, kMultiGather = 2, kMultiSingle = 3;
+
+int multi_row_group(const doci_ham *h, size_t elem) {
+  // every vector's row staged in shared memory: the group is what fits
+  // beside the static tables (at most 212 KB of rows), up to 4
   const size_t row_bytes = static_cast<size_t>((h->max_row + 3) & ~3) * elem;
   const int fit = static_cast<int>((212u * 1024u) / row_bytes);
+  return !row_kernel_fits(h, elem) || fit < 2 ? 0 : fit < 4 ? fit : 4;
+}
+
+int multi_method_auto(const doci_ham *h, int precision) {
+  const size_t elem = precision == DOCI_FP64 ? 8 : 4;
   // same choice of family as the single-vector dispatch
   const bool want_row = h->sigma_kernel >= 2 || (h->sigma_kernel == 0 && h->nrows >= device_sm_count());
-  const bool row = want_row && row_kernel_fits(h, elem) && fit >= 2;
-  if (row) {
-    const int group = fit < 4 ? fit : 4;
+  if (want_row && multi_row_group(h, elem) >= 2) return kMultiRow;
+  if (!want_row || !row_kernel_fits(h, elem)) return kMultiGather;
+  return kMultiSingle;
+}
+
+int run_multi(const doci_ham *h, int method, const void *x, size_t ldx, void *y, size_t ldy, int nv, int precision,
+              cudaStream_t st) {
+  const size_t elem = precision == DOCI_FP64 ? 8 : 4;
+  const char *xc = static_cast<const char *>(x);
+  char *yc = static_cast<char *>(y);
+  if (method == kMultiRow) {
+    const int group = multi_row_group(h, elem);
+    if (group < 2) return DOCI_ERR_INVALID;
     for (int v0 = 0; v0 < nv; v0 += group) {
       const int k = nv - v0 < group ? nv - v0 : group;
       const void *xv = xc + v0 * ldx * elem;
@@ -960,16 +1010,101 @@ int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, si
     }
     return DOCI_OK;
   }
-  if (!want_row || !row_kernel_fits(h, elem))
+  if (method == kMultiGather)
     return precision == DOCI_FP64 ? launch_gather_multi_typed<double>(h, x, ldx, y, ldy, nv, st)
                                   : launch_gather_multi_typed<float>(h, x, ldx, y, ldy, nv, st);
-  // otherwise one vector at a time
-  for (int v = 0; v < nv; ++v) {
+  for (int v = 0; v < nv; ++v) {  // one vector at a time
     const int r = launch_sigma(h, xc + v * ldx * elem, yc + v * ldy * elem, precision, st, false);
     if (r) return r;
   }
   return DOCI_OK;
 }
+
+}  // namespace
+
+int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, size_t ldy, int nv, int precision,
+                       cudaStream_t st) {
+  if (nv < 1 || nv > 4 || ldx < h->D || ldy < h->D) return DOCI_ERR_INVALID;
+  if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
+  // the block solves stay run-to-run reproducible: no pair form here
+  if (nv == 1) return launch_sigma(h, x, y, precision, st, false);
+  int method = h->sigma_kernel == 0 ? tuned_choice(h, precision, nv, false) : 0;
+  if (method == 0) method = multi_method_auto(h, precision);
+  return run_multi(h, method, x, ldx, y, ldy, nv, precision, st);
+}
+
+int autotune_sigma(doci_ham *h, int precision, int nv, cudaStream_t st, int *choice) {
+  if (nv < 1 || nv > 4 || (precision != DOCI_FP64 && precision != DOCI_FP32)) return DOCI_ERR_INVALID;
+  const size_t elem = precision == DOCI_FP64 ? 8 : 4, D = h->D;
+  void *buf = nullptr;
+  DOCI_CUDA(cudaMallocAsync(&buf, 2 * D * nv * elem, st));
+  char *x = static_cast<char *>(buf), *y = x + D * nv * elem;
+  DOCI_CUDA(cudaMemsetAsync(x, 0, D * nv * elem, st));  // the timing does not depend on the values
+  cudaEvent_t e0, e1;
+  DOCI_CUDA(cudaEventCreate(&e0));
+  DOCI_CUDA(cudaEventCreate(&e1));
+  const int saved = h->sigma_kernel;
+  doci_ham *hm = const_cast<doci_ham *>(h);
+  auto time_it = [&](auto &&run) -> double {
+    if (run() != DOCI_OK) return 1e30;  // warm-up; a path that does not apply is skipped
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 2; ++r)
+      if (run() != DOCI_OK) return 1e30;
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms;
+  };
+  int best = 0;
+  if (nv == 1) {
+    for (int allow = 0; allow < 2; ++allow) {
+      double best_ms = 1e30;
+      int pick = 0;
+      for (int kind : {1, 3, 4, 6}) {
+        if (kind == 6 && (!allow || precision != DOCI_FP32)) continue;
+        hm->sigma_kernel = kind;
+        const SigmaPlan p = plan_sigma(h, precision, allow != 0);
+        if (p.kind != kind) continue;  // the path does not fit this shape
+        const double ms = time_it([&] { return launch_sigma(h, x, y, precision, st, allow != 0); });
+        if (ms < best_ms) {
+          best_ms = ms;
+          pick = kind;
+        }
+      }
+      hm->sigma_kernel = saved;
+      if (pick) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tuned[tune_key(h, precision, 1, allow != 0)] = pick;
+      }
+      if (allow) best = pick;
+    }
+  } else {
+    double best_ms = 1e30;
+    hm->sigma_kernel = 0;
+    for (int method : {kMultiRow, kMultiGather, kMultiSingle}) {
+      if (method == kMultiRow && multi_row_group(h, elem) < 2) continue;
+      const double ms = time_it([&] { return run_multi(h, method, x, D, y, D, nv, precision, st); });
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = method;
+      }
+    }
+    hm->sigma_kernel = saved;
+    if (best) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tuned[tune_key(h, precision, nv, false)] = best;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  DOCI_CUDA(cudaFreeAsync(buf, st));
+  DOCI_CUDA(cudaStreamSynchronize(st));
+  if (choice) *choice = best;
+  return best ? DOCI_OK : DOCI_ERR_INVALID;
+}
+
+bool sigma_tuned(const doci_ham *h, int precision, int nv) { return tuned_choice(h, precision, nv, false) != 0; }
 
 int launch_diagonal(doci_ham *h, cudaStream_t st) {
   const SigmaShape s{h->D, h->L, h->N, h->nh};

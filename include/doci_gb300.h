@@ -183,6 +183,19 @@ int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int
  * to 1 when the handle has no row tiling.  For tests and tuning. */
 int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
 
+/* Autotuning: time the sigma paths that fit this handle's shape and keep
+ * the fastest for every handle of the same (device, L, N, precision) in the
+ * process (used when the handle's kind is 0, automatic).  nvec = 1 tunes the
+ * single sigma (doci_sigma, doci_solve; *choice = the kind picked, with the
+ * pair form allowed) and the pair-free path of the block solves; nvec = 2..4
+ * tunes the block sigma of nvec vectors (doci_sigma_block, doci_solve_roots
+ * with that many roots; *choice = 1 row pass in groups, 2 gather, 3 one
+ * vector at a time).  Synchronous; a few sigma calls per candidate.  The
+ * choices change which kernels run, so results computed before and after a
+ * tuning may differ in their last bits; tune before a batch whose results
+ * are compared to single solves.  No counterpart in the reference. */
+int doci_ham_autotune(doci_ham *ham, int precision, int nvec, int *choice);
+
 /* The path doci_sigma takes for this handle and precision: *kind as in
  * doci_ham_set_sigma_kernel (1..6; the automatic choice resolved) and
  * *launches, the number of kernel launches of one call.  Host-only query. */

@@ -257,3 +257,31 @@ def test_sigma_host_pinned_and_pageable(prec_name, synth, dg):
             st = lib.doci_sigma_host(h.handle, C.c_void_p(src.data_ptr()), C.c_void_p(ys[off:].data_ptr()), prec)
             assert st == 0
             assert torch.equal(ys[off:off + D], ref), (pinned, off)
+
+
+def test_autotune_keeps_parity(synth, dg):
+    """doci_ham_autotune picks a path that fits, the plan reports it, sigma on
+    the tuned path still matches the oracle, and a second handle of the same
+    shape uses the same choice; block sigmas after tuning match too."""
+    torch = torch_cuda()
+    p = synth(20, 10, 71)
+    o = oracle.Ham(p)
+    with dg.Hamiltonian.from_fcidump(p) as h, dg.Hamiltonian.from_fcidump(synth(20, 10, 72)) as h2:
+        for prec, tol in ((dg.FP32, TOL32), (dg.FP64, TOL64)):
+            kind = h.autotune(prec, 1)
+            assert kind in (1, 3, 4, 6)
+            assert h.sigma_plan(prec)[0] == kind and h2.sigma_plan(prec)[0] == kind
+            x = np.random.default_rng(7).standard_normal(h.D)
+            yr = o.matvec(x)
+            y = h.sigma(x.astype(np.float32) if prec == dg.FP32 else x, prec)
+            assert np.abs(y - yr).max() <= tol * np.abs(yr).max()
+            method = h.autotune(prec, 3)
+            assert method in (1, 2, 3)
+            tdt = torch.float64 if prec == dg.FP64 else torch.float32
+            X = torch.from_numpy(np.random.default_rng(8).standard_normal((3, h.D))).to(tdt).cuda()
+            Y = torch.empty_like(X)
+            h.sigma_block_device(X.data_ptr(), h.D, Y.data_ptr(), h.D, 3, prec)
+            torch.cuda.synchronize()
+            for v in range(3):
+                ref = o.matvec(X[v].double().cpu().numpy())
+                assert np.abs(Y[v].double().cpu().numpy() - ref).max() <= tol * np.abs(ref).max()
