@@ -4,7 +4,8 @@ oracle/_ref/libdoci_ref.so, the reference itself compiled from its sources
 (present only where the reference checkout was available at build time).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use this
-module, as the checker.  The product (doci_gb300/) never imports it.
+module, to check results and to time the CPU path.  The product (doci_gb300/)
+never imports it.
 """
 from __future__ import annotations
 

@@ -4,8 +4,9 @@
  * TEST INFRASTRUCTURE ONLY.  This library is a plain-C restatement of the
  * reference algorithm (klgunst/doci, src/doci.c, src/davidson.c, src/CG.c,
  * src/read_fcidump.c).  It is used by tests/, by __graft_entry__.smoke() and by
- * the cpu_baseline / --impl reference legs of bench.py as the checker.  The
- * product (doci_gb300/) never links, loads or calls it.
+ * the cpu_baseline / --impl reference legs of bench.py, to check results and
+ * to time the CPU path.  The product (doci_gb300/) never links, loads or calls
+ * it.
  *
  * Parity pins: the oracle is checked (tests/test_oracle_pins.py) against
  *   - the published energies and Davidson traces in tests/coHF.out, lifHF.out;
