@@ -475,13 +475,16 @@ def main():
     achieved = bytes_alg / mean_launch / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", f"sigma_{a.precision}_L{a.L}_N{a.N}.json")
+    limiter = None
     if os.path.exists(prof):
         with open(prof) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            pj = json.load(f)
+        traffic = pj.get("dram_bytes_per_launch")
+        limiter = {"what": pj.get("limiter"), **pj.get("same_kernel_L28_ncu_full", {})} if pj.get("limiter") else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                "bytes_per_det": (2 * nv + 1) * esize, "mean_launch_ms": round(mean_launch * 1e3, 4)}
+                "limiter": limiter, "bytes_per_det": (2 * nv + 1) * esize, "mean_launch_ms": round(mean_launch * 1e3, 4)}
     e2e = None
     if not a.no_e2e:
         hx = torch.randn(D, dtype=tdt, generator=torch.Generator().manual_seed(5)).pin_memory()
