@@ -122,7 +122,8 @@ int fp64_check(MatvecOp &op, const double *d_x, size_t D, double *d_y, double *d
   // r = y - theta x with the residual pass (coefficient 1 on x and y)
   const double one = 1.0;
   DOCI_CUDA(cudaMemcpyAsync(d_red + 8, &one, sizeof(double), cudaMemcpyHostToDevice, st));
-  if ((s = vec_residual<double>(d_x, d_y, D, 1, d_red + 8, *theta, op.ham->d_diag, D, d_r, nullptr, dp, st)))
+  if ((s = vec_residual<double>(d_x, d_y, D, 1, d_red + 8, *theta, op.ham->d_diag, D, d_r, nullptr, dp, st,
+                                op.ham32 ? op.shift32 : 0.0)))
     return s;
   if ((s = vec_reduce(dp, 3, d_red + 16, st))) return s;
   DOCI_CUDA(cudaMemcpyAsync(h_red, d_red + 16, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -475,6 +476,7 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
       op.shift32 = sv64.shift;
       op.x32 = static_cast<float *>(x32.p);
       op.y32 = static_cast<float *>(y32.p);
+      a.shift = sv64.shift;  // the FP64 phase works on H - shift as well
     }
     int its64 = 0;
     for (int round = 0;; ++round) {
@@ -487,6 +489,7 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
       double theta = 0, rnorm = 0;
       double *d_y = static_cast<double *>(scratch.p), *d_r = d_y + D, *dp = d_r + D;
       if ((s = fp64_check(op, d_x, D, d_y, d_r, dp, st, &theta, &rnorm))) return s;
+      theta += sv64.shift;  // op's operator is H - shift
       ++its64;
       out.energy = theta;
       out.residual = rnorm;

@@ -86,9 +86,11 @@ int MatvecOp::apply(const void *d_x, void *d_y, int precision, cudaStream_t st) 
       const double *x = static_cast<const double *>(d_x);
       s = vec_convert<double, float>(x, x32, n, st);
       if (s == DOCI_OK) s = launch_sigma(ham32, x32, y32, DOCI_FP32, st);
-      if (s == DOCI_OK) s = vec_unshift(y32, shift32, x, static_cast<double *>(d_y), n, st);
+      if (s == DOCI_OK) s = vec_convert<float, double>(y32, static_cast<double *>(d_y), n, st);
     } else {
       s = launch_sigma(ham, d_x, d_y, precision, st);
+      if (s == DOCI_OK && ham32 && precision == DOCI_FP64)
+        s = vec_axpy(-shift32, static_cast<const double *>(d_x), static_cast<double *>(d_y), n, st);
     }
     anchor_next = false;
     if (events_on) {
@@ -195,14 +197,14 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
   const bool mixed_sigmas = op.ham32 != nullptr && sizeof(S) == 8;
   std::vector<double> werr(maxv, 0.0);
   auto column = [&](int j) -> int {
-    DOCI_TRY(vec_multidot<S>(Vp, D, j + 1, VAp + static_cast<size_t>(j) * D, D, dp, st));
+    DOCI_TRY(vec_multidot<S>(Vp, D, j + 1, VAp + static_cast<size_t>(j) * D, D, dp, st, false, mixed_sigmas));
     DOCI_TRY(fetch(j + 1));
     for (int i = 0; i <= j; ++i) Sm[j * maxv + i] = red[i];
     bool other = false;
     for (int i = 0; i < j; ++i) other = other || werr[i] < werr[j];
     if (!other) return DOCI_OK;
     std::vector<double> a(red.begin(), red.begin() + j + 1);
-    DOCI_TRY(vec_multidot<S>(VAp, D, j + 1, Vp + static_cast<size_t>(j) * D, D, dp, st));
+    DOCI_TRY(vec_multidot<S>(VAp, D, j + 1, Vp + static_cast<size_t>(j) * D, D, dp, st, false, mixed_sigmas));
     DOCI_TRY(fetch(j + 1));
     for (int i = 0; i < j; ++i) Sm[j * maxv + i] = werr[i] < werr[j] ? red[i] : a[i];
     return DOCI_OK;
@@ -214,15 +216,15 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
       DOCI_TRY(vec_multidot<S>(d_t, D, 1, d_t, D, dp, st));
       DOCI_TRY(fetch(1));
       DOCI_TRY(vec_gs_finish<S>(Vp, D, 0, nullptr, 1.0 / std::sqrt(red[0]), D, d_t, Vm, dp, st));
-    } else if (sizeof(S) == 4 && t_norm2 - proj2 > 0.5 * t_norm2) {
+    } else if ((sizeof(S) == 4 || mixed_sigmas) && t_norm2 - proj2 > 0.5 * t_norm2) {
       // FP32 basis: t keeps more than half of its norm after one projection,
       // so one classical Gram-Schmidt pass is enough (the Daniel-Gragg-
       // Kaufman-Stewart criterion); the residual pass already gave V^T t
       DOCI_CUDA(cudaMemcpyAsync(d_vec, c.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
-      DOCI_TRY(vec_gs_finish<S>(Vp, D, m, d_vec, 1.0 / std::sqrt(t_norm2 - proj2), D, d_t, Vm, dp, st));
+      DOCI_TRY(vec_gs_finish<S>(Vp, D, m, d_vec, 1.0 / std::sqrt(t_norm2 - proj2), D, d_t, Vm, dp, st, mixed_sigmas));
     } else {
       DOCI_CUDA(cudaMemcpyAsync(d_vec, c.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
-      DOCI_TRY(vec_gs_update<S>(Vp, D, m, d_vec, D, d_t, dp, st));
+      DOCI_TRY(vec_gs_update<S>(Vp, D, m, d_vec, D, d_t, dp, st, mixed_sigmas));
       DOCI_TRY(fetch(m + 1));
       double n2 = red[0];
       for (int i = 0; i < m; ++i) {
@@ -231,7 +233,7 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
       }
       if (!(n2 > 0)) n2 = red[0] > 0 ? red[0] : 1.0;
       DOCI_CUDA(cudaMemcpyAsync(d_vec, c.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
-      DOCI_TRY(vec_gs_finish<S>(Vp, D, m, d_vec, 1.0 / std::sqrt(n2), D, d_t, Vm, dp, st));
+      DOCI_TRY(vec_gs_finish<S>(Vp, D, m, d_vec, 1.0 / std::sqrt(n2), D, d_t, Vm, dp, st, mixed_sigmas));
     }
     // ---- the one matvec of the iteration (davidson.c:76)
     DOCI_TRY(op.apply(Vm, VAp + static_cast<size_t>(m) * D, precision, st));
@@ -257,7 +259,7 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
     // ---- residual, preconditioner, first GS projections (davidson.c:90, :98)
     const double theta = w[0];
     DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
-    DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, theta, d_diag, D, d_t, nullptr, dp, st, a.shift));
+    DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, theta, d_diag, D, d_t, nullptr, dp, st, a.shift, mixed_sigmas));
     DOCI_TRY(fetch(m + 2));
     res = std::sqrt(red[0]);
     t_norm2 = red[1];

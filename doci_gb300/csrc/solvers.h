@@ -26,6 +26,11 @@ struct MatvecOp {
   // vectors, whose coefficients in the Ritz vector are of the size of the
   // residual) run on the shifted FP32 view: y = sigma32((float)x) + shift x.
   // Their FP32 rounding enters the Ritz vector scaled by those coefficients.
+  // With ham32 set the operator is the shifted H - shift32 (both paths): the
+  // anchor's FP64 sigma gets -shift32 x added, the FP32 sigma of the view is
+  // already shifted.  The FP64 phase then works, like the FP32 phase, with
+  // quantities of the size of H - shift32, so its FP32-arithmetic correction
+  // terms stay accurate.
   const doci_ham *ham32 = nullptr;
   double shift32 = 0;
   float *x32 = nullptr, *y32 = nullptr;  // D-element scratch, owned by the caller

@@ -439,6 +439,165 @@ combine_f32_kernel(const float *__restrict__ V, size_t ld, int m, const double *
   }
 }
 
+// ---- FP64-storage passes with mixed arithmetic (FP64 phase of the mixed
+// mode, whose correction vectors carry FP32-accurate sigmas) ----------------
+// Column 0 of the basis (the anchor: the run's start vector, after a restart
+// the lowest Ritz vector) is handled in FP64; columns >= 1 (corrections,
+// whose coefficients are of the size of the residual) in FP32 arithmetic
+// with FP64 accumulation of the reductions, as the FP32 passes above.  The
+// FP32 rounding of a correction term then enters scaled by its small
+// coefficient, like the FP32 rounding of its sigma.
+
+template <int K>
+__global__ void __launch_bounds__(f32_block<K>())
+multidot_mix_kernel(const double *__restrict__ V, size_t ld, int m, const double *__restrict__ w, size_t n,
+                    double *__restrict__ partials) {
+  __shared__ double acc_s[K * f32_block<K>()];
+  SmemAcc<K, f32_block<K>()> acc{acc_s};
+  acc.zero();
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  double a0 = 0;
+  for (size_t j0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j0 < n; j0 += stride * kChunk) {
+    float f[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) f[k] = 0.f;
+    for (int u = 0; u < kChunk; ++u) {
+      const size_t j = j0 + u * stride;
+      if (j >= n) break;
+      const double wj = w[j];
+      a0 = fma(V[j], wj, a0);
+      const float wf = static_cast<float>(wj);
+#pragma unroll
+      for (int k = 1; k < K; ++k)
+        if (k < m) f[k] = fmaf(static_cast<float>(V[k * ld + j]), wf, f[k]);
+    }
+    acc.add(f, m);
+  }
+  acc.a[threadIdx.x] = a0;  // column 0's slot holds its FP64 sum (the FP32 chunks left it at 0)
+  acc.store(m, partials);
+}
+
+template <int K>
+__global__ void __launch_bounds__(f32_block<K>())
+residual_mix_kernel(const double *__restrict__ V, const double *__restrict__ VA, size_t ld, int m,
+                    const double *__restrict__ y, double theta, double pre_theta, const double *__restrict__ diag,
+                    size_t n, double *__restrict__ t, double *__restrict__ x_out, double *__restrict__ partials) {
+  __shared__ float ys[K];
+  __shared__ double acc_s[(K + 2) * f32_block<K>()];
+  if (threadIdx.x < K) ys[threadIdx.x] = threadIdx.x < m ? static_cast<float>(y[threadIdx.x]) : 0.f;
+  SmemAcc<K + 2, f32_block<K>()> acc{acc_s};
+  acc.zero();
+  __syncthreads();
+  const double y0 = y[0];
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  double r2 = 0, t2 = 0, d0 = 0;  // FP64: ||r||^2, ||t||^2, V_0 . t
+  for (size_t j0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j0 < n; j0 += stride * kChunk) {
+    float f[K + 2];
+#pragma unroll
+    for (int k = 0; k < K + 2; ++k) f[k] = 0.f;
+    for (int u = 0; u < kChunk; ++u) {
+      const size_t j = j0 + u * stride;
+      if (j >= n) break;
+      float v[K];
+      float xs = 0.f, as = 0.f;  // correction parts
+#pragma unroll
+      for (int k = 1; k < K; ++k)
+        if (k < m) {
+          v[k] = static_cast<float>(V[k * ld + j]);
+          xs = fmaf(v[k], ys[k], xs);
+          as = fmaf(static_cast<float>(VA[k * ld + j]), ys[k], as);
+        }
+      const double v0 = V[j];
+      const double xv = fma(v0, y0, static_cast<double>(xs));
+      const double av = fma(VA[j], y0, static_cast<double>(as));
+      const double r = av - theta * xv;
+      r2 = fma(r, r, r2);
+      if (x_out) x_out[j] = xv;
+      const double d = fabs(diag[j] - pre_theta);
+      const double tv = d > 1e-12 ? r / d : r / 1e-12;  // davidson.c:214-227
+      t[j] = tv;
+      t2 = fma(tv, tv, t2);
+      d0 = fma(v0, tv, d0);
+      const float tf = static_cast<float>(tv);
+#pragma unroll
+      for (int k = 1; k < K; ++k)
+        if (k < m) f[2 + k] = fmaf(v[k], tf, f[2 + k]);
+    }
+    acc.add(f, m + 2);
+  }
+  acc.a[0 * f32_block<K>() + threadIdx.x] = r2;
+  acc.a[1 * f32_block<K>() + threadIdx.x] = t2;
+  acc.a[2 * f32_block<K>() + threadIdx.x] = d0;
+  acc.store(m + 2, partials);
+}
+
+template <int K>
+__global__ void __launch_bounds__(f32_block<K>())
+gs_update_mix_kernel(const double *__restrict__ V, size_t ld, int m, const double *__restrict__ c, size_t n,
+                     double *__restrict__ t, double *__restrict__ partials) {
+  __shared__ float cs[K];
+  __shared__ double acc_s[(K + 1) * f32_block<K>()];
+  if (threadIdx.x < K) cs[threadIdx.x] = threadIdx.x < m ? static_cast<float>(c[threadIdx.x]) : 0.f;
+  SmemAcc<K + 1, f32_block<K>()> acc{acc_s};
+  acc.zero();
+  __syncthreads();
+  const double c0 = c[0];
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  double t2 = 0, d0 = 0;
+  for (size_t j0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j0 < n; j0 += stride * kChunk) {
+    float f[K + 1];
+#pragma unroll
+    for (int k = 0; k < K + 1; ++k) f[k] = 0.f;
+    for (int u = 0; u < kChunk; ++u) {
+      const size_t j = j0 + u * stride;
+      if (j >= n) break;
+      float v[K];
+      float cs_sum = 0.f;
+#pragma unroll
+      for (int k = 1; k < K; ++k)
+        if (k < m) {
+          v[k] = static_cast<float>(V[k * ld + j]);
+          cs_sum = fmaf(cs[k], v[k], cs_sum);
+        }
+      const double v0 = V[j];
+      const double tv = t[j] - fma(c0, v0, static_cast<double>(cs_sum));
+      t[j] = tv;
+      t2 = fma(tv, tv, t2);
+      d0 = fma(v0, tv, d0);
+      const float tf = static_cast<float>(tv);
+#pragma unroll
+      for (int k = 1; k < K; ++k)
+        if (k < m) f[1 + k] = fmaf(v[k], tf, f[1 + k]);
+    }
+    acc.add(f, m + 1);
+  }
+  acc.a[0 * f32_block<K>() + threadIdx.x] = t2;
+  acc.a[1 * f32_block<K>() + threadIdx.x] = d0;
+  acc.store(m + 1, partials);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kT)
+gs_finish_mix_kernel(const double *__restrict__ V, size_t ld, int m, const double *__restrict__ c, double scale,
+                     size_t n, const double *__restrict__ t, double *__restrict__ out,
+                     double *__restrict__ partials) {
+  __shared__ float cs[K];
+  if (threadIdx.x < K) cs[threadIdx.x] = threadIdx.x < m ? static_cast<float>(c[threadIdx.x]) : 0.f;
+  __syncthreads();
+  const double c0 = m > 0 ? c[0] : 0.0;
+  double acc[1] = {0};
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    float cs_sum = 0.f;
+#pragma unroll
+    for (int k = 1; k < K; ++k)
+      if (k < m) cs_sum = fmaf(cs[k], static_cast<float>(V[k * ld + j]), cs_sum);
+    const double o = (t[j] - fma(c0, V[j], static_cast<double>(cs_sum))) * scale;
+    out[j] = o;
+    acc[0] = fma(o, o, acc[0]);
+  }
+  block_reduce_store<1>(acc, 1, partials);
+}
+
 template <typename A, typename B>
 __global__ void convert_kernel(const A *__restrict__ a, B *__restrict__ b, size_t n) {
   for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
@@ -616,6 +775,37 @@ struct MultidotL {
   }
 };
 template <typename S, int K>
+struct MultidotMixL {
+  static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const S *w, size_t n, double *p) {
+    if constexpr (std::is_same<S, double>::value)
+      multidot_mix_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, ld, m, w, n, p);
+  }
+};
+template <typename S, int K>
+struct ResidualMixL {
+  static void run(int g, cudaStream_t st, const S *V, const S *VA, size_t ld, int m, const double *y, double th,
+                  double pre, const double *diag, size_t n, S *t, double *x, double *p) {
+    if constexpr (std::is_same<S, double>::value)
+      residual_mix_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, VA, ld, m, y, th, pre, diag, n,
+                                                                              t, x, p);
+  }
+};
+template <typename S, int K>
+struct GsUpdateMixL {
+  static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *p) {
+    if constexpr (std::is_same<S, double>::value)
+      gs_update_mix_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, ld, m, c, n, t, p);
+  }
+};
+template <typename S, int K>
+struct GsFinishMixL {
+  static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, double sc, size_t n,
+                  const S *t, S *out, double *p) {
+    if constexpr (std::is_same<S, double>::value)
+      gs_finish_mix_kernel<K><<<wave_grid(gs_finish_mix_kernel<K>, kT), kT, 0, st>>>(V, ld, m, c, sc, n, t, out, p);
+  }
+};
+template <typename S, int K>
 struct MultidotExactL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const S *w, size_t n, double *p) {
     multidot_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, w, n, p);
@@ -724,6 +914,19 @@ int vec_copy(void *dst, const void *src, size_t bytes, cudaStream_t st) {
   return DOCI_OK;
 }
 
+namespace {
+__global__ void axpy_kernel(double a, const double *__restrict__ x, double *__restrict__ y, size_t n) {
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    y[j] = fma(a, x[j], y[j]);
+}
+}  // namespace
+
+int vec_axpy(double a, const double *x, double *y, size_t n, cudaStream_t st) {
+  axpy_kernel<<<grid_blocks(), kT, 0, st>>>(a, x, y, n);
+  DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
 int vec_unshift(const float *y32, double shift, const double *x, double *y, size_t n, cudaStream_t st) {
   unshift_kernel<<<grid_blocks(), kT, 0, st>>>(y32, shift, x, y, n);
   DOCI_CUDA(cudaGetLastError());
@@ -744,31 +947,38 @@ int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st) {
 
 template <typename S>
 int vec_multidot(const S *V, size_t ld, int m, const S *w, size_t n, double *partials, cudaStream_t st,
-                 bool fp64_products) {
+                 bool fp64_products, bool mixed) {
   if (m < 1 || m > 32) return DOCI_ERR_INVALID;
+  if (mixed && std::is_same<S, double>::value) return dispatch_k<S, MultidotMixL>(m, st, V, ld, m, w, n, partials);
   if (fp64_products) return dispatch_k<S, MultidotExactL>(m, st, V, ld, m, w, n, partials);
   return dispatch_k<S, MultidotL>(m, st, V, ld, m, w, n, partials);
 }
 template <typename S>
 int vec_residual(const S *V, const S *VA, size_t ld, int m, const double *y, double theta, const double *diag,
-                 size_t n, S *t, double *x, double *partials, cudaStream_t st, double diag_shift) {
+                 size_t n, S *t, double *x, double *partials, cudaStream_t st, double diag_shift, bool mixed) {
   if (m < 1 || m > 32) return DOCI_ERR_INVALID;
+  if (mixed && std::is_same<S, double>::value)
+    return dispatch_k<S, ResidualMixL>(m, st, V, VA, ld, m, y, theta, theta + diag_shift, diag, n, t, x, partials);
   return dispatch_k<S, ResidualL>(m, st, V, VA, ld, m, y, theta, theta + diag_shift, diag, n, t, x, partials);
 }
 template <typename S>
-int vec_gs_update(const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *partials, cudaStream_t st) {
+int vec_gs_update(const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *partials, cudaStream_t st,
+                  bool mixed) {
   if (m < 1 || m > 32) return DOCI_ERR_INVALID;
+  if (mixed && std::is_same<S, double>::value) return dispatch_k<S, GsUpdateMixL>(m, st, V, ld, m, c, n, t, partials);
   return dispatch_k<S, GsUpdateL>(m, st, V, ld, m, c, n, t, partials);
 }
 template <typename S>
 int vec_gs_finish(const S *V, size_t ld, int m, const double *c, double scale, size_t n, const S *t, S *out,
-                  double *partials, cudaStream_t st) {
+                  double *partials, cudaStream_t st, bool mixed) {
   if (m < 0 || m > 32) return DOCI_ERR_INVALID;
   if (m == 0) {
     scale_kernel<S><<<grid_blocks(), kT, 0, st>>>(t, scale, out, n);
     DOCI_CUDA(cudaGetLastError());
     return DOCI_OK;
   }
+  if (mixed && std::is_same<S, double>::value)
+    return dispatch_k<S, GsFinishMixL>(m, st, V, ld, m, c, scale, n, t, out, partials);
   return dispatch_k<S, GsFinishL>(m, st, V, ld, m, c, scale, n, t, out, partials);
 }
 template <typename S>
@@ -844,12 +1054,14 @@ int precond_inverse(const double *diag, double *pinv, size_t n, cudaStream_t st)
 }
 
 #define DOCI_VEC_INST(S)                                                                                   \
-  template int vec_multidot<S>(const S *, size_t, int, const S *, size_t, double *, cudaStream_t, bool);    \
+  template int vec_multidot<S>(const S *, size_t, int, const S *, size_t, double *, cudaStream_t, bool,     \
+                               bool);                                                                       \
   template int vec_residual<S>(const S *, const S *, size_t, int, const double *, double, const double *,   \
-                               size_t, S *, double *, double *, cudaStream_t, double);                      \
-  template int vec_gs_update<S>(const S *, size_t, int, const double *, size_t, S *, double *, cudaStream_t); \
+                               size_t, S *, double *, double *, cudaStream_t, double, bool);                \
+  template int vec_gs_update<S>(const S *, size_t, int, const double *, size_t, S *, double *, cudaStream_t, \
+                                bool);                                                                      \
   template int vec_gs_finish<S>(const S *, size_t, int, const double *, double, size_t, const S *, S *,      \
-                                double *, cudaStream_t);                                                    \
+                                double *, cudaStream_t, bool);                                              \
   template int vec_deflate<S>(S *, size_t, int, int, const double *, int, size_t, cudaStream_t);            \
   template int vec_combine<S>(const S *, size_t, int, const double *, size_t, double *, cudaStream_t);
 DOCI_VEC_INST(double)

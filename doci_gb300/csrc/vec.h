@@ -22,24 +22,29 @@ int vec_reduce(const double *partials, int nk, double *out, cudaStream_t st);
 
 template <typename S>
 int vec_multidot(const S *V, size_t ld, int m, const S *w, size_t n, double *partials, cudaStream_t st,
-                 bool fp64_products = false);  // FP32 storage: true = exact products, FP64 sums
+                 bool fp64_products = false,  // FP32 storage: true = exact products, FP64 sums
+                 bool mixed = false);         // FP64 storage: column 0 in FP64, the rest in FP32 arithmetic
 template <typename S>
 int vec_residual(const S *V, const S *VA, size_t ld, int m, const double *y, double theta, const double *diag,
-                 size_t n, S *t, double *x, double *partials, cudaStream_t st, double diag_shift = 0.0);
+                 size_t n, S *t, double *x, double *partials, cudaStream_t st, double diag_shift = 0.0,
+                 bool mixed = false);
 // index of the smallest element (first on ties), synchronous
 int vec_argmin(const double *d, size_t n, int64_t *idx, cudaStream_t st);
 // bytes from src to dst by a kernel (both device-accessible: device memory or
 // pinned host memory mapped into the device's address space)
 int vec_copy(void *dst, const void *src, size_t bytes, cudaStream_t st);
+// y += a x (FP64)
+int vec_axpy(double a, const double *x, double *y, size_t n, cudaStream_t st);
 // y[j] = y32[j] + shift x[j]: an FP32 sigma of H - shift back to H, in FP64
 int vec_unshift(const float *y32, double shift, const double *x, double *y, size_t n, cudaStream_t st);
 // out[j] = (float)(d[j] - shift): the FP32 diagonal of the shifted operator H - shift
 int vec_shifted_diag32(const double *d, double shift, float *out, size_t n, cudaStream_t st);
 template <typename S>
-int vec_gs_update(const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *partials, cudaStream_t st);
+int vec_gs_update(const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *partials, cudaStream_t st,
+                  bool mixed = false);
 template <typename S>
 int vec_gs_finish(const S *V, size_t ld, int m, const double *c, double scale, size_t n, const S *t, S *out,
-                  double *partials, cudaStream_t st);
+                  double *partials, cudaStream_t st, bool mixed = false);
 template <typename S>
 int vec_deflate(S *V, size_t ld, int mv, int keep, const double *Y, int ldy, size_t n, cudaStream_t st);
 template <typename S>
