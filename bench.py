@@ -261,9 +261,12 @@ def cpu_sample(path: str, seconds: float, seed: int = 0):
     nchunks = 64
 
     def run(total: int):
-        per = max(1, total // nchunks)
-        first = np.array([(c * (D - per)) // (nchunks - 1) for c in range(nchunks)], dtype=np.uint64)
-        length = np.full(nchunks, per, dtype=np.uint64)
+        # nch evenly spread chunks of `per` determinants (fewer for small spaces)
+        total = max(1, min(total, D))
+        nch = min(nchunks, total)
+        per = max(1, total // nch)
+        first = np.array([(c * (D - per)) // max(1, nch - 1) for c in range(nch)], dtype=np.uint64)
+        length = np.full(nch, per, dtype=np.uint64)
         rows = np.concatenate([np.arange(f, f + per, dtype=np.int64) for f in first])
         diag = np.concatenate([h.diagonal_range(int(f), per) for f in first])
         t0 = time.perf_counter()
@@ -271,10 +274,10 @@ def cpu_sample(path: str, seconds: float, seed: int = 0):
         dt = time.perf_counter() - t0
         return len(rows), dt
 
-    n0, t0 = run(64 * 2048)
+    n0, t0 = run(min(64 * 2048, D))
     rate = n0 / max(t0, 1e-6)
     total = int(min(rate * seconds, D))
-    n, dt = run(max(total, 64 * 2048))
+    n, dt = run(max(total, min(64 * 2048, D)))
     return {"dets": n, "seconds": dt, "rate": n / dt, "threads": threads, "D": D, "run": run}
 
 
@@ -521,7 +524,7 @@ def main():
                 "warmup": a.warmup, "ms_per_step": round(total / a.steps * 1e3, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == dg.FP32 else "f64",
                 "data": "synthetic (seeded FCIDUMP of the benchmark integral model)",
-                "config": {"workload": f"DOCI sigma L={a.L} N={a.N} D={D} seed={a.seed} {a.precision}"
+                "config": {"workload": f"DOCI sigma L={a.L} N={a.N} D={D} seed={a.seed}"
                                        + (f" block of {nv} vectors" if nv > 1 else ""),
                            "block": nv,
                            "L": a.L, "N": a.N, "D": D, "seed": a.seed, "precision": a.precision,
@@ -554,8 +557,9 @@ def reference_arm(a, ws, rank):
     line = {"metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": 0, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": round(total / a.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"DOCI sigma L={a.L} N={a.N} D={s['D']} seed={a.seed} (bounded CPU sample)",
-                       "L": a.L, "N": a.N, "D": s["D"], "seed": a.seed},
+            "config": {"workload": f"DOCI sigma L={a.L} N={a.N} D={s['D']} seed={a.seed}",
+                       "L": a.L, "N": a.N, "D": s["D"], "seed": a.seed, "precision": "fp64",
+                       "sample": "bounded CPU sample per step (cpu_baseline.sample)"},
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": s["threads"], "kind": "port",
                              "sample": f"{s['dets']} determinants per step in 64 evenly spread chunks, FP64 "
