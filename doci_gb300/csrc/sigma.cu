@@ -1044,7 +1044,7 @@ int autotune_sigma(doci_ham *h, int precision, int nv, cudaStream_t st, int *cho
   DOCI_CUDA(cudaEventCreate(&e0));
   DOCI_CUDA(cudaEventCreate(&e1));
   const int saved = h->sigma_kernel;
-  doci_ham *hm = const_cast<doci_ham *>(h);
+  doci_ham *hm = h;
   auto time_it = [&](auto &&run) -> double {
     if (run() != DOCI_OK) return 1e30;  // warm-up; a path that does not apply is skipped
     cudaEventRecord(e0, st);

@@ -882,14 +882,6 @@ __global__ void shifted_diag_kernel(const double *__restrict__ d, double shift, 
 }  // namespace
 
 namespace {
-__global__ void unshift_kernel(const float *__restrict__ y32, double shift, const double *__restrict__ x,
-                               double *__restrict__ y, size_t n) {
-  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
-    y[j] = static_cast<double>(y32[j]) + shift * x[j];
-}
-}  // namespace
-
-namespace {
 __global__ void copy16_kernel(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n) {
   for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
     dst[j] = src[j];
@@ -927,11 +919,6 @@ int vec_axpy(double a, const double *x, double *y, size_t n, cudaStream_t st) {
   return DOCI_OK;
 }
 
-int vec_unshift(const float *y32, double shift, const double *x, double *y, size_t n, cudaStream_t st) {
-  unshift_kernel<<<grid_blocks(), kT, 0, st>>>(y32, shift, x, y, n);
-  DOCI_CUDA(cudaGetLastError());
-  return DOCI_OK;
-}
 
 int vec_shifted_diag32(const double *d, double shift, float *out, size_t n, cudaStream_t st) {
   shifted_diag_kernel<<<grid_blocks(), kT, 0, st>>>(d, shift, out, n);

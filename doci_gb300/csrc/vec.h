@@ -35,8 +35,6 @@ int vec_argmin(const double *d, size_t n, int64_t *idx, cudaStream_t st);
 int vec_copy(void *dst, const void *src, size_t bytes, cudaStream_t st);
 // y += a x (FP64)
 int vec_axpy(double a, const double *x, double *y, size_t n, cudaStream_t st);
-// y[j] = y32[j] + shift x[j]: an FP32 sigma of H - shift back to H, in FP64
-int vec_unshift(const float *y32, double shift, const double *x, double *y, size_t n, cudaStream_t st);
 // out[j] = (float)(d[j] - shift): the FP32 diagonal of the shifted operator H - shift
 int vec_shifted_diag32(const double *d, double shift, float *out, size_t n, cudaStream_t st);
 template <typename S>
