@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libdoci_ref.so")
 REF_EXE_PATH = os.path.join(HERE, "_ref", "doci_ref")
+REF_EXE_PLAIN_PATH = os.path.join(HERE, "_ref", "doci_ref_plain")
 _pd = C.POINTER(C.c_double)
 _pu64 = C.POINTER(C.c_uint64)
 

@@ -230,9 +230,12 @@ static double diag_one(const orc_ham *h, const int *occ) {
 }
 
 void orc_diagonal_range(const orc_ham *h, uint64_t first, uint64_t count, double *out) {
-  int occ[65];
-  for (uint64_t r = 0; r < count; ++r) {
-    occ_of(orc_unrank(first + r, h->L, h->N), h->L, occ);
+  /* large ranges are split over the host threads (a call from inside a
+   * parallel region runs on its own thread) */
+#pragma omp parallel for schedule(static) if (count > 65536)
+  for (long long r = 0; r < (long long)count; ++r) {
+    int occ[65];
+    occ_of(orc_unrank(first + (uint64_t)r, h->L, h->N), h->L, occ);
     out[r] = diag_one(h, occ);
   }
 }

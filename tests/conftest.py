@@ -55,6 +55,12 @@ def synth(tmp_path_factory):
     return get
 
 
+def reference_dir() -> str:
+    """The reference checkout ($DOCI_REFERENCE, else `reference` beside the
+    repository); tests that read it skip where it is absent."""
+    return os.environ.get("DOCI_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
 def cuda_ok() -> bool:
     try:
         import torch

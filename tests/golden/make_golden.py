@@ -1,9 +1,17 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference itself.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>   (or $DOCI_REFERENCE)
+    python tests/golden/make_golden.py --ref <...> --config2 [--threads T]
 
 Needs the reference checkout (its tests/ FCIDUMPs and sources) and builds
 oracle/_ref (the reference compiled from its own sources, oracle/Makefile).
+--exe only (re)makes exe/*.out: the reference executable's stdout
+(EXE_CASES below), built with and without -DDAVIDIT, run on one thread.
+--config2 only (re)makes the entry "synthetic_L28_N14_s2" of golden.json:
+the reference executable's Davidson (DAVIDSON_MAX_VEC 30, DAVIDSON_KEEP 2,
+TOL 1e-8, HF start) and CGP (MAX_ITS 40) runs on the seeded L=28, N=14
+Hamiltonian (D = 40,116,600), with their iteration traces and wall times on
+T OpenMP threads (several minutes of CPU; about 20 GB of host memory).
 Writes:
   molecules/<name>.FCIDUMP.gz   the reference's test integrals (tests/*.FCIDUMP),
                                 gzipped, so GPU runs without the checkout can
@@ -33,6 +41,7 @@ import shutil
 import subprocess
 import sys
 import tempfile
+import time
 
 import numpy as np
 
@@ -46,25 +55,96 @@ from doci_gb300.fcidump import write_synthetic_fcidump  # noqa: E402
 MOLECULES = ["H2O_STO3G", "N2_STO3G", "H2O_631G", "lili_321g", "lif_631g_1", "co_631g_1"]
 
 
-def run_ref_exe(fcidump: str, solver: str, max_its: int, tol: float = 1e-8) -> dict:
+def run_ref_exe(fcidump: str, solver: str, max_its: int, tol: float = 1e-8, threads: int = 4,
+                extra: str = "", timed: bool = False) -> dict:
     with tempfile.TemporaryDirectory() as td:
         inp = os.path.join(td, "in.in")
         with open(inp, "w") as f:
-            f.write(f"FCIDUMP= {fcidump}\nSOLVER = {solver}\nMAX_ITS={max_its}\nTOL={tol:g}\nHF_INIT= 1\n")
-        env = dict(os.environ, OMP_NUM_THREADS="4", OPENBLAS_NUM_THREADS="1")
+            f.write(f"FCIDUMP= {fcidump}\nSOLVER = {solver}\nMAX_ITS={max_its}\nTOL={tol:g}\nHF_INIT= 1\n{extra}")
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1")
+        t0 = time.perf_counter()
         out = subprocess.run([oracle.REF_EXE_PATH, inp], capture_output=True, text=True, env=env, check=True).stdout
+        wall = time.perf_counter() - t0
     rows = re.findall(r"^(\d+)\t(\d+)\t(\S+)\t(\S+)$", out, re.M)
     energy = float(re.search(r"\*\* DOCI ENERGY : (\S+)", out).group(1))
     code = int(re.search(r"\*\* EXIT CODE SOLVER : (\S+)", out).group(1))
-    return {"energy_printed": energy, "exit_code": code,
-            "trace": [[int(a), float(c), float(d)] for a, b, c, d in rows]}
+    r = {"energy_printed": energy, "exit_code": code,
+         "trace": [[int(a), float(c), float(d)] for a, b, c, d in rows]}
+    if timed:
+        r["wall_s"] = round(wall, 2)
+        r["threads"] = threads
+    return r
+
+
+# name, molecule, input keys (besides FCIDUMP); the input echo names the
+# FCIDUMP by the relative path "<molecule>.FCIDUMP"
+EXE_CASES = [
+    ("H2O_631G_D", "H2O_631G", "SOLVER = D\nTOL = 1e-8\nHF_INIT = 1\n"),
+    ("H2O_631G_CGP", "H2O_631G", "SOLVER = CGP\nMAX_ITS = 60\nTOL = 1e-8\n"),
+    ("lif_631g_1_D", "lif_631g_1", "SOLVER = D\nMAX_ITS = 100\nTOL = 1e-8\nDAVIDSON_KEEP = 2\n"
+                                   "DAVIDSON_MAX_VEC = 30\nHF_INIT = 1\n"),
+    ("co_631g_1_D", "co_631g_1", "SOLVER = D\nTOL = 1e-8\nDAVIDSON_MAX_VEC = 12\nDAVIDSON_KEEP = 3\n"),
+]
+
+
+def exe_outputs(ref: str) -> None:
+    out_dir = os.path.join(HERE, "exe")
+    os.makedirs(out_dir, exist_ok=True)
+    env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
+    for name, mol, keys in EXE_CASES:
+        with tempfile.TemporaryDirectory() as td:
+            shutil.copy(os.path.join(ref, "tests", mol + ".FCIDUMP"), os.path.join(td, mol + ".FCIDUMP"))
+            with open(os.path.join(td, "in.in"), "w") as f:
+                f.write(f"FCIDUMP = {mol}.FCIDUMP\n{keys}")
+            for exe, tag in ((oracle.REF_EXE_PATH, "davidit"), (oracle.REF_EXE_PLAIN_PATH, "plain")):
+                r = subprocess.run([exe, "in.in"], capture_output=True, text=True, env=env, cwd=td, check=True)
+                with open(os.path.join(out_dir, f"{name}.{tag}.out"), "w") as f:
+                    f.write(r.stdout)
+        print(name, flush=True)
+
+
+def config2(ref: str, threads: int) -> None:
+    """The plain FP64 Davidson and CGP of the L=28, N=14 Hamiltonian (seed 2)
+    through the reference executable; merged into golden.json."""
+    L, N, seed = 28, 14, 2
+    with tempfile.TemporaryDirectory() as td:
+        p = os.path.join(td, f"synthetic_L{L}_N{N}_s{seed}.FCIDUMP")
+        write_synthetic_fcidump(p, L, N, seed)
+        dav = run_ref_exe(p, "D", 1000, threads=threads, extra="DAVIDSON_KEEP = 2\nDAVIDSON_MAX_VEC = 30\n",
+                          timed=True)
+        print("D", dav["energy_printed"], len(dav["trace"]), dav["wall_s"], flush=True)
+        cgp = run_ref_exe(p, "CGP", 40, threads=threads, timed=True)
+        print("CGP", cgp["energy_printed"], len(cgp["trace"]), cgp["wall_s"], flush=True)
+    gp = os.path.join(HERE, "golden.json")
+    with open(gp) as f:
+        golden = json.load(f)
+    golden["cases"][f"synthetic_L{L}_N{N}_s{seed}"] = {
+        "L": L, "N": N, "D": 40116600, "seed": seed, "generated": "doci_gb300.fcidump.write_synthetic_fcidump",
+        "D_exe": dav, "CGP_exe": cgp,
+        "settings": {"D": "DAVIDSON_MAX_VEC 30, DAVIDSON_KEEP 2, TOL 1e-8, HF_INIT 1, MAX_ITS 1000",
+                     "CGP": "TOL 1e-8, HF_INIT 1, MAX_ITS 40"},
+        "host": f"{os.cpu_count()} cores ({threads} OpenMP threads), OPENBLAS_NUM_THREADS=1"}
+    with open(gp, "w") as f:
+        json.dump(golden, f, indent=1)
 
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("DOCI_REFERENCE"),
+                    help="reference checkout (default: $DOCI_REFERENCE)")
+    ap.add_argument("--config2", action="store_true", help="only the L=28, N=14 entry")
+    ap.add_argument("--exe", action="store_true", help="only the executable's stdout fixtures")
+    ap.add_argument("--threads", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give --ref or set DOCI_REFERENCE")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={a.ref}", "all", "ref"], check=True)
+    if a.config2:
+        config2(a.ref, a.threads)
+        return
+    if a.exe:
+        exe_outputs(a.ref)
+        return
     mol_dir = os.path.join(HERE, "molecules")
     os.makedirs(mol_dir, exist_ok=True)
     cases = {}

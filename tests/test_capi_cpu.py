@@ -11,7 +11,7 @@ import sys
 import numpy as np
 import pytest
 
-from conftest import ROOT, cuda_ok
+from conftest import ROOT, cuda_ok, reference_dir
 
 HEADER = os.path.join(ROOT, "include", "doci_gb300.h")
 
@@ -38,7 +38,7 @@ def test_header_symbols_exported(lib):
     assert not missing, missing
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="reference sources not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(reference_dir(), "src")), reason="reference sources not present")
 def test_reference_executable_links(lib, tmp_path):
     """The reference's executable.c + macros.c link against libdoci_gb300 in place of doci.c."""
     import glob
@@ -46,7 +46,7 @@ def test_reference_executable_links(lib, tmp_path):
     ob = glob.glob(os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs", "libscipy_openblas*.so"))
     if not ob:
         pytest.skip("no BLAS")
-    R = "/root/reference"
+    R = reference_dir()
     exe = str(tmp_path / "doci_ref_on_gpu")
     pkg = os.path.join(ROOT, "doci_gb300")
     cmd = ["gcc", "-O2", "-Dnone=shared", f"-I{R}/include", "-Ddnrm2_=scipy_dnrm2_", "-Ddscal_=scipy_dscal_",

@@ -128,3 +128,19 @@ def test_gather_rows_matches_matvec(synth):
     rows = np.concatenate([np.arange(f, f + n) for f, n in zip(first, length)]).astype(np.int64)
     yr = o.gather_rows(x, first, length, o.diag[rows])
     assert np.abs(yr - y[rows]).max() <= 1e-12 * np.abs(y).max()
+
+
+@pytest.mark.parametrize("L,N,seed", [(20, 10, 41), (22, 6, 42)])
+def test_gather_rows_matches_matvec_whole_space(L, N, seed, synth):
+    """The gather form (prefix-sum neighbour ranks) that checks the sampled
+    rows of the full-size GPU tests, against the reference-order matvec
+    (direct ranks, symmetric scatter, doci.c:164-238) on every row of a
+    mid-size space."""
+    p = synth(L, N, seed)
+    o = oracle.Ham(p)
+    x = np.random.default_rng(seed).standard_normal(o.D)
+    y = o.matvec(x)
+    first = np.array([0], dtype=np.uint64)
+    length = np.array([o.D], dtype=np.uint64)
+    yr = o.gather_rows(x, first, length, o.diag)
+    assert np.abs(yr - y).max() <= 1e-12 * np.abs(y).max()

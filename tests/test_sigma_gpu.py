@@ -153,6 +153,36 @@ def test_sigma_L32_fp32_vs_oracle_samples(kernel, synth, dg):
         assert bad.size == 0, (kernel, int(rows[bad[0]]), float(got[bad[0]]), float(ref[bad[0]]), int(bad.size))
 
 
+@pytest.mark.parametrize("kernel", ["auto", "rowx", "gather"])
+def test_sigma_L32_fp64_vs_oracle_samples(kernel, synth, dg):
+    """L=32, N=16 (D = 601,080,390), FP64 (the anchor and verification sigma
+    of every mixed solve at this size): sampled rank windows across the whole
+    space against the FP64 oracle gather form, 1e-12 of the largest |sigma|."""
+    torch = torch_cuda()
+    p = synth(32, 16, 3)
+    o = oracle.Ham(p, keep_diag=False)
+    with dg.Hamiltonian.from_fcidump(p) as h:
+        D = h.D
+        h.set_sigma_kernel(kernel)
+        g = torch.Generator(device="cuda").manual_seed(11)
+        x = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
+        y = torch.empty_like(x)
+        h.sigma_device(x.data_ptr(), y.data_ptr(), dg.FP64)
+        torch.cuda.synchronize()
+        first = np.array([0, 12_870, 150_000_000, 300_540_000, 450_000_000, D - 20_000, D - 1000],
+                         dtype=np.uint64)
+        length = np.full(len(first), 1000, dtype=np.uint64)
+        rows = np.concatenate([np.arange(f, f + n) for f, n in zip(first, length)]).astype(np.int64)
+        idx = torch.from_numpy(rows).cuda()
+        xs = x.cpu().numpy()
+        ref = o.gather_rows(xs, first, length, h.diagonal()[rows])
+        got = y[idx].cpu().numpy()
+        del x, y
+        err = np.abs(got - ref)
+        bad = np.nonzero(err > 1e-12 * np.abs(ref).max())[0]
+        assert bad.size == 0, (kernel, int(rows[bad[0]]), float(got[bad[0]]), float(ref[bad[0]]), int(bad.size))
+
+
 def test_default_stream_orders_after_caller_work(synth, dg):
     """A NULL stream is CUDA's default stream: a sigma queued right after the
     caller's own kernels on it sees their results (x written by randn)."""
