@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--N", type=int, default=16)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
-    ap.add_argument("--kernel", choices=["auto", "gather", "row", "row1", "rowx", "rowxc", "pair", "pairsmem"], default="auto")
+    ap.add_argument("--kernel", choices=["auto", "gather", "row1", "rowx", "pair", "tc"], default="auto")
     ap.add_argument("--block", type=int, default=1,
                     help="sigma: vectors per step through doci_sigma_block (1 = doci_sigma)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
@@ -396,7 +396,7 @@ def serve_workload(a):
     print(json.dumps(line), flush=True)
 
 
-KERNEL_NAMES = {1: "gather", 2: "row", 3: "row1", 4: "rowx", 5: "rowxc", 6: "pair", 7: "pairsmem"}
+KERNEL_NAMES = {1: "gather", 3: "row1", 4: "rowx", 6: "pair", 8: "tc"}
 
 
 def solve_workload(a):

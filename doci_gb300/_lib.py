@@ -168,6 +168,10 @@ def default_opts(**kw) -> SolveOpts:
     return o
 
 
+KERNEL_KINDS = {"auto": 0, "gather": 1, "row1": 3, "rowx": 4, "pair": 6, "tc": 8}
+KERNEL_NAMES = {v: k for k, v in KERNEL_KINDS.items()}
+
+
 class Hamiltonian:
     """A DOCI Hamiltonian resident on the current CUDA device (doci_ham)."""
 
@@ -217,8 +221,9 @@ class Hamiltonian:
         self.close()
 
     def set_sigma_kernel(self, kind) -> None:
-        """0/'auto', 1/'gather', 2/'row' (row + column-panel passes), 3/'row1' (row pass only)."""
-        kind = {"auto": 0, "gather": 1, "row": 2, "row1": 3, "rowx": 4, "rowxc": 5, "pair": 6, "pairsmem": 7}.get(kind, kind)
+        """0/'auto', 1/'gather', 3/'row1' (row pass), 4/'rowx' (phase-ordered row pass),
+        6/'pair' (pair form, mma.sync), 8/'tc' (pair form, tcgen05); doci_ham_set_sigma_kernel."""
+        kind = KERNEL_KINDS.get(kind, kind)
         _check(lib().doci_ham_set_sigma_kernel(self._h, int(kind)), "doci_ham_set_sigma_kernel")
 
     def diagonal(self) -> np.ndarray:

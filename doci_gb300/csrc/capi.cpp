@@ -276,7 +276,7 @@ int doci_ham_autotune(doci_ham *h, int precision, int nvec, int *choice) {
 }
 
 int doci_ham_set_sigma_kernel(doci_ham *h, int kind) {
-  if (!h || kind < 0 || kind > 7) return DOCI_ERR_INVALID;
+  if (!h || !(kind == 0 || kind == 1 || kind == 3 || kind == 4 || kind == 6 || kind == 8)) return DOCI_ERR_INVALID;
   h->sigma_kernel = kind;
   return DOCI_OK;
 }
@@ -305,7 +305,7 @@ int doci_sigma_host(doci_ham *h, const void *x, void *y, int precision) {
     DOCI_CUDA(cudaMemcpyAsync(y, h->d_stage_y, bytes, cudaMemcpyDeviceToHost, h->stream));
   }
   DOCI_CUDA(cudaStreamSynchronize(h->stream));
-  return DOCI_OK;
+  return ham_device_error(h, h->stream);
 }
 
 int doci_bitstrings(doci_ham *h, int64_t first, int64_t count, uint32_t *d_bits, void *stream) {
@@ -529,7 +529,7 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
   res->sigma_seconds = op.sigma_seconds;
   if (vec) DOCI_CUDA(cudaMemcpyAsync(vec, d_x, sizeof(double) * D, cudaMemcpyDeviceToHost, st));
   DOCI_CUDA(cudaStreamSynchronize(st));
-  return DOCI_OK;
+  return ham_device_error(h, st);
 }
 
 // ===========================================================================

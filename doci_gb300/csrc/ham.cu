@@ -51,12 +51,25 @@ static void release_async(void *p, cudaStream_t st) {
   if (p) cudaFreeAsync(p, st);
 }
 
+// The error word of the tensor-core sigma's bounded device waits: read on the
+// stream (synchronising it), cleared; DOCI_ERR_DEVICE_TIMEOUT when a wait ran
+// out since the last check.
+int ham_device_error(doci_ham *h, cudaStream_t st) {
+  if (!h->d_tc_err) return DOCI_OK;
+  int v = 0;
+  DOCI_CUDA(cudaMemcpyAsync(&v, h->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  DOCI_CUDA(cudaStreamSynchronize(st));
+  if (v == 0) return DOCI_OK;
+  DOCI_CUDA(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), st));
+  DOCI_CUDA(cudaStreamSynchronize(st));
+  return DOCI_ERR_DEVICE_TIMEOUT;
+}
+
 void ham_release(doci_ham *h) {
   if (!h) return;
   cudaStream_t st = h->stream;
   void *bufs[] = {h->d_binom, h->d_Kmir64, h->d_Kmir32, h->d_tab64, h->d_diag, h->d_diag32, h->d_stage_x,
-                  h->d_stage_y, h->d_rows, h->d_rowstart, h->d_sector_rs, h->d_sector_off, h->d_panels[0],
-                  h->d_panels[1], h->d_pblocks, h->d_kfrag};  // d_rem/d_ins/d_tab_off are shared (per-process cache)
+                  h->d_stage_y, h->d_rows, h->d_rowstart, h->d_pblocks, h->d_kfrag, h->d_tc_err};  // d_rem/d_ins/d_tab_off are shared (per-process cache)
   for (void *p : bufs) release_async(p, st);
   if (h->h_diag) cudaFreeHost(h->h_diag);
   if (st) {
@@ -67,11 +80,10 @@ void ham_release(doci_ham *h) {
   h->d_Kmir64 = h->d_tab64 = h->d_diag = nullptr;
   h->d_Kmir32 = h->d_diag32 = nullptr;
   h->d_stage_x = h->d_stage_y = nullptr;
-  h->d_rows = h->d_rowstart = h->d_sector_rs = nullptr;
-  h->d_sector_off = nullptr;
-  h->d_panels[0] = h->d_panels[1] = nullptr;
+  h->d_rows = h->d_rowstart = nullptr;
   h->d_pblocks = nullptr;
   h->d_kfrag = nullptr;
+  h->d_tc_err = nullptr;
   h->npblocks = 0;
   h->d_rem = h->d_ins = h->d_tab_off = nullptr;
   h->h_diag = nullptr;
@@ -162,6 +174,8 @@ int ham_build(doci_ham *h, const Integrals &in) {
   DOCI_CUDA(cudaMallocAsync(&h->d_tab64, tab.size() * sizeof(double), h->stream));
   DOCI_CUDA(cudaMallocAsync(&h->d_diag, static_cast<size_t>(h->D) * sizeof(double), h->stream));
   DOCI_CUDA(cudaMallocAsync(&h->d_diag32, static_cast<size_t>(h->D) * sizeof(float), h->stream));
+  DOCI_CUDA(cudaMallocAsync(&h->d_tc_err, sizeof(int), h->stream));
+  DOCI_CUDA(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_binom, binom.data(), binom.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_Kmir64, kmir.data(), kmir.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_Kmir32, kmir32.data(), kmir32.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
@@ -229,25 +243,6 @@ int ham_build_rows(doci_ham *h) {
   }
   h->nrows = static_cast<int>(order.size());
   h->max_row = max_row;
-  // sector lists: sector k holds the row-part sets with k elements; the set
-  // with colex rank g sits at index C(na, k) - 1 - g
-  std::vector<uint32_t> sector(size_t(1) << na, 0xffffffffu);
-  int off = 0, max_sector = 0;
-  for (int k = 0; k <= na; ++k) {
-    h->sector_off[k] = off;
-    const int cnt = static_cast<int>(binom64(na, k));
-    if (N - k >= 0 && N - k <= split && cnt > max_sector) max_sector = cnt;
-    off += cnt;
-  }
-  h->sector_off[na + 1] = off;
-  for (uint32_t mask = 0; mask < (1u << na); ++mask) {
-    const int k = __builtin_popcount(mask);
-    uint64_t colex = 0;
-    for (int a = 0, t = 0; a < na; ++a)
-      if (mask >> a & 1u) colex += binom64(a, ++t);
-    sector[h->sector_off[k] + (binom64(na, k) - 1 - colex)] = start[mask];
-  }
-  h->max_sector_rows = max_sector;
   DOCI_CUDA(cudaMallocAsync(&h->d_rows, rows.size() * sizeof(uint32_t), h->stream));
   DOCI_CUDA(cudaMallocAsync(&h->d_rowstart, start.size() * sizeof(uint32_t), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_rows, rows.data(), rows.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
@@ -277,25 +272,6 @@ int ham_build_rows(doci_ham *h) {
     h->d_ins = it->second[1];
     h->d_tab_off = it->second[2];
   }
-  DOCI_CUDA(cudaMallocAsync(&h->d_sector_off, sizeof(h->sector_off), h->stream));
-  DOCI_CUDA(cudaMemcpyAsync(h->d_sector_off, h->sector_off, sizeof(h->sector_off), cudaMemcpyHostToDevice, h->stream));
-  for (int v = 0; v < 2; ++v) {  // column panels of 2 (FP64) or 4 (FP32) columns
-    const int W = v == 0 ? 2 : 4;
-    std::vector<int2> pv;
-    for (int k = 0; k <= na; ++k) {
-      const int j = N - k;
-      if (j < 0 || j > split) continue;
-      const uint64_t ncol = binom64(split, j);
-      for (uint64_t c0 = 0; c0 < ncol; c0 += W) pv.push_back(make_int2(k, static_cast<int>(c0)));
-    }
-    h->npanels[v] = static_cast<int>(pv.size());
-    DOCI_CUDA(cudaMallocAsync(&h->d_panels[v], pv.size() * sizeof(int2), h->stream));
-    DOCI_CUDA(cudaMemcpyAsync(h->d_panels[v], pv.data(), pv.size() * sizeof(int2), cudaMemcpyHostToDevice, h->stream));
-    DOCI_CUDA(cudaStreamSynchronize(h->stream));
-  }
-  DOCI_CUDA(cudaMallocAsync(&h->d_sector_rs, sector.size() * sizeof(uint32_t), h->stream));
-  DOCI_CUDA(cudaMemcpyAsync(h->d_sector_rs, sector.data(), sector.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                            h->stream));
   DOCI_CUDA(cudaStreamSynchronize(h->stream));
   return ham_build_pairs(h, start);
 }

@@ -85,26 +85,21 @@ struct doci_ham {
   int nrows = 0;
   int max_row = 0;                // largest row length
   uint32_t *d_rows = nullptr;     // nrows x {rowstart, mask | k << 24}
-  int sigma_kernel = 0;           // 0 automatic, 1 per-determinant gather, 2 row kernel
+  int sigma_kernel = 0;           // doci_ham_set_sigma_kernel's kind (0 automatic)
   uint32_t *d_rowstart = nullptr; // 2^(L - split) entries: row start by row-part mask
-  // column-panel pass (row-part hops): rows of each sector (fixed |row part|)
-  // listed by reversed colex of the row-part set
-  uint32_t *d_sector_rs = nullptr; // sum_k C(L - split, k) row starts
-  int sector_off[33] = {};         // offset of sector k in d_sector_rs
-  int max_sector_rows = 0;
-  int *d_sector_off = nullptr;     // sector_off on the device
-  int2 *d_panels[2] = {};          // column panels {k, c0}: [0] FP64 (2 columns), [1] FP32 (4 columns)
-  int npanels[2] = {};
   // cross-hop index tables of the phase-ordered row pass (addressing.cuh,
   // build_cross_tables)
   uint32_t *d_rem = nullptr, *d_ins = nullptr, *d_tab_off = nullptr;
   // pair form (sigma_pair.cu): one block per (N-1)-pair set's row part R',
   // {own row start or ~0, mask | k' << 24}, largest first; the K matrix split
-  // into TF32 high and low parts (2 x 32 x 32 floats)
+  // into TF32 high and low parts (2 x 32 x 32 floats, mirrored orbitals; also
+  // the B operand of the tensor-core pair form, sigma_tc.cu)
   uint32_t *d_pblocks = nullptr;
   int npblocks = 0;
   void *d_kfrag = nullptr;
 
+  // error word of the tensor-core sigma's bounded waits (0 = none)
+  int *d_tc_err = nullptr;
   // host diagonal for doci_get_diagonal (lazy)
   double *h_diag = nullptr;
   // device staging for the host-buffer entry points (lazy)
@@ -119,9 +114,10 @@ namespace doci {
 int ham_build(doci_ham *h, const Integrals &in);
 void ham_release(doci_ham *h);
 int ham_stage(doci_ham *h, size_t bytes);
+int ham_device_error(doci_ham *h, cudaStream_t st);
 // sigma.cu
-// The kernel path of a sigma: kind as doci_ham_set_sigma_kernel (1..6) and
-// the number of kernel launches it takes.
+// The kernel path of a sigma: kind as doci_ham_set_sigma_kernel (1, 3, 4, 6,
+// 8) and the number of kernel launches it takes.
 struct SigmaPlan {
   int kind, launches;
 };
@@ -144,7 +140,14 @@ int launch_sigma_multi(const doci_ham *h, const void *x, size_t ldx, void *y, si
 int kernel_blocks(const void *kernel, int threads, size_t dyn, int *blocks);
 // pair-form sigma (sigma_pair.cu), FP32 only
 bool pair_fits(const doci_ham *h);
-int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t s, bool lean);
+int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t s);
+// tensor-core pair form (sigma_tc.cu), FP32 only, sm_103a; x 16-byte aligned.
+// A device wait that runs out writes a nonzero code to *d_err (spin_limit:
+// try_wait iterations per wait).
+constexpr long kTcSpinLimit = 1L << 20;  // try_wait polls per wait (seconds at most)
+bool tc_fits(const doci_ham *h);
+int tc_launches(const doci_ham *h);
+int launch_tc(const doci_ham *h, const float *x, float *y, cudaStream_t s, int *d_err, long spin_limit);
 int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &row_start);
 int launch_bitstrings(const doci_ham *h, int64_t first, int64_t count, uint32_t *out, cudaStream_t s);
 int launch_ranks(const doci_ham *h, const uint32_t *bits, int64_t count, int64_t *out, cudaStream_t s);

@@ -10,6 +10,8 @@
 // no partial vectors, sigma written once with coalesced stores.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <mutex>
 #include <map>
 #include <tuple>
@@ -754,125 +756,6 @@ bool rowx_fits(const doci_ham *h, size_t elem) {
   return 2 * (static_cast<size_t>(h->max_row) + 3) * elem <= 210 * 1024;
 }
 
-// ---------------------------------------------------------------------------
-// Column-panel pass: the row-part hops (both orbitals in the row part) keep
-// the column and change the row, within one sector (rows with the same
-// number k of row-part elements).  One block loads W consecutive columns of
-// every row of a sector into shared memory (panel[row][w]), so each x element
-// is read once per pass, and each thread gathers its row's k (na - k)
-// neighbour rows from the panel, W columns per load.  Sector-local row index
-// = C(na, k) - 1 - colex of the row-part set, so the neighbour machinery of
-// addressing.cuh gives neighbour indices directly.  Adds into y (the row
-// pass has written diagonal, column-part and cross hops).
-// ---------------------------------------------------------------------------
-constexpr int kColThreads = 256;
-
-struct ColShape {
-  int L, N, split, na;
-};
-
-template <typename Real, int W>
-struct Vec;
-template <>
-struct Vec<float, 4> {
-  using T = float4;
-};
-template <>
-struct Vec<double, 2> {
-  using T = double2;
-};
-
-template <typename Real, int W, int NHA>
-__global__ void __launch_bounds__(kColThreads)
-sigma_col_kernel(ColShape s, const int2 *__restrict__ panels, int npanels, const uint32_t *__restrict__ sector_rs,
-                 const int *__restrict__ sector_off, const uint32_t *__restrict__ g_binom,
-                 const Real *__restrict__ g_K, const Real *__restrict__ x, Real *__restrict__ y) {
-  __shared__ uint32_t binom[kBinomRows * kBinomCols];
-  __shared__ Real K[32 * 32];
-  extern __shared__ __align__(16) unsigned char col_smem[];
-  Real *P = reinterpret_cast<Real *>(col_smem);
-  for (int t = threadIdx.x; t < kBinomRows * kBinomCols; t += blockDim.x) binom[t] = g_binom[t];
-  for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) K[t] = g_K[t];
-  const int sp = s.split, na = s.na;
-  for (int pi = blockIdx.x; pi < npanels; pi += gridDim.x) {
-    const int2 pn = panels[pi];
-    const int k = pn.x, j = s.N - k;
-    const uint32_t c0 = static_cast<uint32_t>(pn.y);
-    __syncthreads();
-    const uint32_t ncol = binom[sp * kBinomCols + j];
-    const uint32_t wc = ncol - c0 < static_cast<uint32_t>(W) ? ncol - c0 : static_cast<uint32_t>(W);
-    const uint32_t nr = binom[na * kBinomCols + k];
-    const uint32_t *rs = sector_rs + sector_off[k];
-    for (uint32_t t = threadIdx.x; t < nr * W; t += blockDim.x) {
-      const uint32_t r = t / W, w = t % W;
-      if (w < wc) cp_async<sizeof(Real)>(P + t, x + rs[r] + c0 + w);
-      else P[t] = Real(0);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    const Real *Kbase = K + sp * 32 + sp;
-    for (uint32_t r = threadIdx.x; r < nr; r += blockDim.x) {
-      const uint32_t R = nr - 1 - r;
-      const uint32_t M = dev::colex_unrank<kBinomCols>(R, na, k, binom);
-      dev::Neighbours<NHA, kBinomCols> nb;
-      nb.precompute(M, R, na, na - k, binom);
-      struct Acc {
-        const Real *Kb, *P;
-        const Real *Krow;
-        Real a[W];
-        __device__ __forceinline__ void begin(int m) { Krow = Kb + m * 32; }
-        __device__ __forceinline__ void hop(int, int q, uint32_t idx) {
-          const typename Vec<Real, W>::T v = *reinterpret_cast<const typename Vec<Real, W>::T *>(P + idx * W);
-          const Real kv = Krow[q];
-          const Real *vv = reinterpret_cast<const Real *>(&v);
-#pragma unroll
-          for (int w = 0; w < W; ++w) a[w] += kv * vv[w];
-        }
-      } f{Kbase, P, Kbase, {}};
-      nb.visit(M, R, nr - 1, k, na - k, binom, f);
-      Real *yo = y + rs[r] + c0;
-#pragma unroll
-      for (int w = 0; w < W; ++w)
-        if (static_cast<uint32_t>(w) < wc) yo[w] += f.a[w];
-    }
-  }
-}
-
-template <typename Real>
-int launch_col(const doci_ham *h, const void *x, void *y, cudaStream_t st) {
-  constexpr int W = sizeof(Real) == 4 ? 4 : 2;
-  const ColShape s{h->L, h->N, h->split, h->L - h->split};
-  const int v = sizeof(Real) == 4 ? 1 : 0;
-  const int2 *d_panels = h->d_panels[v];
-  const int npanels = h->npanels[v];
-  const size_t dyn = static_cast<size_t>(h->max_sector_rows) * W * sizeof(Real);
-  // the neighbour routine keeps one register slot per row-part hole
-  const int kmin = h->N - h->split > 0 ? h->N - h->split : 0;
-  const bool wide = s.na - kmin > 16;
-  int bps = 1;
-  if (wide) {
-    DOCI_TRY_S(blocks_for(sigma_col_kernel<Real, W, 24>, kColThreads, dyn, &bps));
-  } else {
-    DOCI_TRY_S(blocks_for(sigma_col_kernel<Real, W, 16>, kColThreads, dyn, &bps));
-  }
-  auto kern = wide ? sigma_col_kernel<Real, W, 24> : sigma_col_kernel<Real, W, 16>;
-  int grid = device_sm_count() * bps;
-  if (grid > npanels) grid = npanels;
-  const Real *K = std::is_same<Real, double>::value ? reinterpret_cast<const Real *>(h->d_Kmir64)
-                                                   : reinterpret_cast<const Real *>(h->d_Kmir32);
-  kern<<<grid, kColThreads, dyn, st>>>(s, d_panels, npanels, h->d_sector_rs, h->d_sector_off, h->d_binom, K,
-                                       static_cast<const Real *>(x), static_cast<Real *>(y));
-  DOCI_CUDA(cudaGetLastError());
-  return DOCI_OK;
-}
-
-bool col_pass_fits(const doci_ham *h, size_t elem) {
-  const int W = elem == 4 ? 4 : 2;
-  const int na = h->L - h->split;
-  if (na < 1 || na > 32 || na - 0 > 24) return false;
-  return static_cast<size_t>(h->max_sector_rows) * W * elem <= 210 * 1024;
-}
-
 unsigned grid_for(uint64_t n) {
   uint64_t g = (n + kThreads - 1) / kThreads;
   const uint64_t cap = static_cast<uint64_t>(device_sm_count()) * 8;
@@ -914,27 +797,24 @@ int tuned_choice(const doci_ham *h, int precision, int nv, bool allow_pair) {
 // does not fit falls back as described at doci_ham_set_sigma_kernel.
 SigmaPlan plan_kind(const doci_ham *h, int precision, bool allow_pair, int kind) {
   const size_t elem = precision == DOCI_FP64 ? 8 : 4;
-  // pair form: on request (kind 6), and the automatic FP32 choice when its
-  // blocks give every SM work (measured fastest there); FP32 only
-  const bool want_pair = kind == 6 || kind == 7 || (kind == 0 && h->npblocks >= device_sm_count());
-  if (allow_pair && want_pair && precision == DOCI_FP32 && pair_fits(h))
-    return {kind == 7 ? 7 : 6, 2};  // init pass + pair pass
+  if (precision == DOCI_FP64 && (kind == 6 || kind == 8)) kind = 0;  // FP32-only forms: the automatic FP64 path
+  if (allow_pair && precision == DOCI_FP32) {
+    // tensor-core pair form: the automatic FP32 choice where it fits and the
+    // space gives every SM units of work (measured fastest there)
+    const bool want_tc = kind == 8 || (kind == 0 && h->npblocks >= device_sm_count());
+    if (want_tc && tc_fits(h)) return {8, tc_launches(h)};
+    // mma.sync pair form: on request (kind 6)
+    if (kind == 6 && pair_fits(h)) return {6, 2};  // init pass + pair pass
+  }
   // row kernel when the row tiling exists, fits, and gives every SM work
-  bool row = kind >= 2 || (kind == 0 && h->nrows >= device_sm_count());
+  bool row = kind >= 3 || (kind == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
   if (!row) return {1, 1};
   // automatic: the phase-ordered pass for FP64 (measured faster there), the
   // single row pass for FP32 (measured faster there)
-  const bool want_rowx = kind >= 4 || (kind == 0 && precision == DOCI_FP64);
-  if (want_rowx && rowx_fits(h, elem)) {
-    // kind 5 moves the row-part hops to the column-panel pass
-    const bool colp = kind == 5 && col_pass_fits(h, elem);
-    return colp ? SigmaPlan{5, 2} : SigmaPlan{4, 1};
-  }
-  // row-part hops in the column-panel pass only on request (kind 2): the
-  // single row pass (kind 3, and the automatic choice) measured faster
-  const bool col = kind == 2 && col_pass_fits(h, elem);
-  return col ? SigmaPlan{2, 2} : SigmaPlan{3, 1};
+  const bool want_rowx = kind == 4 || (kind == 0 && precision == DOCI_FP64);
+  if (want_rowx && rowx_fits(h, elem)) return {4, 1};
+  return {3, 1};
 }
 
 }  // namespace
@@ -945,28 +825,37 @@ SigmaPlan plan_sigma(const doci_ham *h, int precision, bool allow_pair) {
   return plan_kind(h, precision, allow_pair, kind);
 }
 
+// try_wait iterations per device wait of the tensor-core sigma; the
+// environment variable DOCI_TC_SPIN_LIMIT (read once) lowers it, so that a
+// test can make every wait run out and check the reported status
+long tc_spin_limit() {
+  static const long v = [] {
+    const char *e = std::getenv("DOCI_TC_SPIN_LIMIT");
+    return e ? std::strtol(e, nullptr, 10) : kTcSpinLimit;
+  }();
+  return v;
+}
+
 int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaStream_t st, bool allow_pair) {
   if (precision != DOCI_FP64 && precision != DOCI_FP32) return DOCI_ERR_INVALID;
   const bool f64 = precision == DOCI_FP64;
   const SigmaPlan p = plan_sigma(h, precision, allow_pair);
-  int r = DOCI_OK;
   switch (p.kind) {
+    case 8:
+      if ((reinterpret_cast<uintptr_t>(x) & 15u) == 0)
+        return launch_tc(h, static_cast<const float *>(x), static_cast<float *>(y), st, h->d_tc_err, tc_spin_limit());
+      // bulk copies need a 16-byte aligned x: the mma.sync pair form instead
+      return pair_fits(h) ? launch_pair(h, static_cast<const float *>(x), static_cast<float *>(y), st)
+                          : launch_row<float>(h, x, y, st, 1);
     case 6:
-    case 7:
-      // kind 6: the lean variant (measured faster: 37 ms against 55 ms at L=32)
-      return launch_pair(h, static_cast<const float *>(x), static_cast<float *>(y), st, p.kind == 6);
+      return launch_pair(h, static_cast<const float *>(x), static_cast<float *>(y), st);
     case 1:
       return f64 ? launch_typed<double>(h, x, y, st) : launch_typed<float>(h, x, y, st);
     case 4:
-    case 5:
-      r = f64 ? launch_rowx<double>(h, x, y, st, p.kind == 5 ? 0 : 1) : launch_rowx<float>(h, x, y, st, p.kind == 5 ? 0 : 1);
-      break;
-    default:  // 2, 3
-      r = f64 ? launch_row<double>(h, x, y, st, p.kind == 2 ? 0 : 1) : launch_row<float>(h, x, y, st, p.kind == 2 ? 0 : 1);
-      break;
+      return f64 ? launch_rowx<double>(h, x, y, st, 1) : launch_rowx<float>(h, x, y, st, 1);
+    default:  // 3
+      return f64 ? launch_row<double>(h, x, y, st, 1) : launch_row<float>(h, x, y, st, 1);
   }
-  if (r || p.launches == 1) return r;
-  return f64 ? launch_col<double>(h, x, y, st) : launch_col<float>(h, x, y, st);
 }
 
 namespace {
@@ -1061,8 +950,8 @@ int autotune_sigma(doci_ham *h, int precision, int nv, cudaStream_t st, int *cho
     for (int allow = 0; allow < 2; ++allow) {
       double best_ms = 1e30;
       int pick = 0;
-      for (int kind : {1, 3, 4, 6}) {
-        if (kind == 6 && (!allow || precision != DOCI_FP32)) continue;
+      for (int kind : {1, 3, 4, 6, 8}) {
+        if ((kind == 6 || kind == 8) && (!allow || precision != DOCI_FP32)) continue;
         hm->sigma_kernel = kind;
         const SigmaPlan p = plan_sigma(h, precision, allow != 0);
         if (p.kind != kind) continue;  // the path does not fit this shape

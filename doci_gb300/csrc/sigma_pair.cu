@@ -1,4 +1,7 @@
-// sigma_pair.cu -- FP32 sigma in the (N-1)-pair intermediate form.
+// sigma_pair.cu -- FP32 sigma in the (N-1)-pair intermediate form on the
+// warp-level mma.sync path (kind 6).  The tensor-core version of the same form,
+// sigma_tc.cu (kind 8), is the automatic FP32 choice on sm_103a; this one
+// stays for x buffers that are not 16-byte aligned and for comparison.
 //
 // Every off-diagonal element of the DOCI Hamiltonian is a pair hop
 // T -> T \ i u a with weight K_ia = (ia|ia) (doci.c:216-222).  Writing
@@ -14,10 +17,9 @@
 //
 // Sets S are grouped by their row part R' (the mirrored orbitals
 // [split, L) of the row tiling): the determinants S u a with a in the
-// column part lie in row R' (one contiguous rank range, accumulated in
-// shared memory and added to sigma once per block), those with a in the row
-// part lie at the same column position of the rows R' u a (coalesced loads
-// and atomic adds).  sigma is first set to diag * x; all hop contributions
+// column part lie in row R' (one contiguous rank range, random accesses and
+// atomic adds within it), those with a in the row part lie at the same column
+// position of the rows R' u a (coalesced loads and atomic adds).  sigma is first set to diag * x; all hop contributions
 // are atomic adds, so the FP32 summation order (and the last bits of the
 // result) varies from run to run.
 #include <cuda_runtime.h>
@@ -44,7 +46,7 @@ struct PairShape {
   int L, N, split, na, nblocks;
 };
 
-struct PairSmem {
+struct PairSmem {  // 49.4 KB of static shared memory
   uint4 kfrag[4 * 4 * 32];                   // this block's K, [k step][n tile][lane]: {b0 hi, b1 hi, b0 lo, b1 lo}
   float tile[kPairWarps][32][kTileStride];   // per warp: X_S then Y_S, column s = the warp's 32 sets
   uint32_t hole_rs[32];                      // row-part holes b of R': start of row R' u b
@@ -80,21 +82,17 @@ __global__ void pair_init_kernel(uint32_t D, const float *__restrict__ diag, con
 // of the column orbitals (column position c in a row of C(split, jp)
 // columns).  The MMA's orbital axis is compacted to the column orbitals
 // followed by the row-part holes of R' (the row-part elements of R' are in
-// every S, so their X entries are zero).
-// kLean (the default, kind 6): own-row sums by global atomics (no row buffer
-// in shared memory), one m-tile of the product at a time and the insertion
-// entries re-read for the scatter, so that four blocks fit an SM (registers
-// <= 64): 32 warps per SM hide the gathers' latency.  !kLean (kind 7): the
-// own row's sums in shared memory, two blocks per SM.  Measured at L=32,
-// N=16: 37.1 ms against 55.0 ms.
-template <bool kLean>
-__global__ void __launch_bounds__(kPairThreads, kLean ? 4 : 2)
+// every S, so their X entries are zero).  Own-row sums by global atomics, one
+// m-tile of the product at a time and the insertion entries re-read for the
+// scatter, so that four blocks fit an SM (registers <= 64): 32 warps per SM
+// hide the gathers' latency (37.1 ms at L=32, N=16, against 55.0 ms with the
+// own row's sums in shared memory and two blocks per SM).
+__global__ void __launch_bounds__(kPairThreads, 4)
 sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t *__restrict__ rowstart_of,
                   const uint32_t *__restrict__ g_binom, const float *__restrict__ g_ksplit,
                   const uint32_t *__restrict__ ins, const uint32_t *__restrict__ ins_off,
                   const float *__restrict__ x, float *__restrict__ y) {
   __shared__ __align__(16) PairSmem sm;
-  extern __shared__ __align__(16) float acc[];  // own row: hop sums into row R'
   const uint32_t *B = g_binom;
   const int sp = s.split;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -110,9 +108,8 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
     const uint32_t own = bw.x, mask = bw.y & 0xffffffu;
     const int kp = static_cast<int>(bw.y >> 24), jp = s.N - 1 - kp;
     const int nhr = s.na - kp, keff = sp + nhr, nk = (keff + 7) >> 3, nch = sp - jp;
-    __syncthreads();  // previous block's flush is done with acc, holes and fragments
+    __syncthreads();  // the previous block is done with the holes and fragments
     const uint32_t n_s = __ldg(B + sp * kBinomCols + jp);
-    const uint32_t n_own = jp + 1 <= sp ? __ldg(B + sp * kBinomCols + jp + 1) : 0u;
     if (warp == 0) {
       const bool hole = lane < s.na && !((mask >> lane) & 1u);
       const uint32_t hb = __ballot_sync(0xffffffffu, hole);
@@ -122,8 +119,6 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
         sm.hole_o[h] = sp + lane;
       }
     }
-    if constexpr (!kLean)
-      for (uint32_t c = threadIdx.x; c < n_own; c += blockDim.x) acc[c] = 0.f;
     __syncthreads();
     for (int e = threadIdx.x; e < 4 * 4 * 32; e += blockDim.x) {
       const int kt = e >> 7, nt = (e >> 5) & 3, ln = e & 31;
@@ -171,54 +166,7 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
       }
       __syncwarp();
       // Y = X K on the tensor cores: 3xTF32 (lo*hi + hi*lo + hi*hi)
-      if constexpr (!kLean) {
-        float cc[2][4][4];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-          for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) cc[mt][nt][e] = 0.f;
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt) {
-          if (kt < nk) {
-            uint32_t ah[2][4], al[2][4];
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-              const int r0 = 16 * mt + g, k0 = 8 * kt + tq;
-              const float f[4] = {tile[k0][r0], tile[k0][r0 + 8], tile[k0 + 4][r0], tile[k0 + 4][r0 + 8]};
-#pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                ah[mt][e] = to_tf32(f[e]);
-                al[mt][e] = to_tf32(f[e] - __uint_as_float(ah[mt][e]));
-              }
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt)
-              if (nt < nk) {
-                const uint4 b = sm.kfrag[(kt * 4 + nt) * 32 + lane];
-#pragma unroll
-                for (int mt = 0; mt < 2; ++mt) {
-                  mma_tf32(cc[mt][nt], al[mt], b.x, b.y);
-                  mma_tf32(cc[mt][nt], ah[mt], b.z, b.w);
-                  mma_tf32(cc[mt][nt], ah[mt], b.x, b.y);
-                }
-              }
-          }
-        }
-        __syncwarp();
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-          for (int nt = 0; nt < 4; ++nt)
-            if (nt < nk) {
-              const int r0 = 16 * mt + g, q0 = 8 * nt + 2 * tq;
-              tile[q0][r0] = cc[mt][nt][0];
-              tile[q0 + 1][r0] = cc[mt][nt][1];
-              tile[q0][r0 + 8] = cc[mt][nt][2];
-              tile[q0 + 1][r0 + 8] = cc[mt][nt][3];
-            }
-      } else {
+      {
         // one m-tile (16 sets) at a time: its rows of the tile are disjoint
         // from the other m-tile's, so its Y may overwrite its X at once
 #pragma unroll
@@ -265,7 +213,7 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
       __syncwarp();
       // scatter Y_S back to the same determinants
       if (live) {
-        if constexpr (kLean) {
+        {
           const uint4 *ip = reinterpret_cast<const uint4 *>(ins_blk + 16u * c);
 #pragma unroll
           for (int u = 0; u < 4; ++u)
@@ -275,18 +223,11 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
         for (int h = 0; h < 16; ++h)
           if (h < nch) {
             const uint32_t e = lane_of(ent[h >> 2], h & 3);
-            if constexpr (kLean)
-              atomicAdd(y + own + (e >> 8), tile[e & 0xffu][lane]);
-            else
-              atomicAdd(&acc[e >> 8], tile[e & 0xffu][lane]);
+            atomicAdd(y + own + (e >> 8), tile[e & 0xffu][lane]);
           }
         for (int h = 0; h < nhr; ++h) atomicAdd(y + sm.hole_rs[h] + c, tile[sp + h][lane]);
       }
       __syncwarp();  // the tile is cleared by the next round
-    }
-    if constexpr (!kLean) {
-      __syncthreads();
-      for (uint32_t c = threadIdx.x; c < n_own; c += blockDim.x) atomicAdd(y + own + c, acc[c]);
     }
   }
 }
@@ -349,7 +290,7 @@ int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
   return DOCI_OK;
 }
 
-int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st, bool lean) {
+int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
   if (!pair_fits(h)) return DOCI_ERR_INVALID;
   const int sms = device_sm_count();
   {
@@ -360,22 +301,14 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st, bo
     DOCI_CUDA(cudaGetLastError());
   }
   const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, h->npblocks};
-  const size_t dyn = lean ? 0 : static_cast<size_t>(h->max_row) * sizeof(float);
-  const void *kern = lean ? reinterpret_cast<const void *>(sigma_pair_kernel<true>)
-                          : reinterpret_cast<const void *>(sigma_pair_kernel<false>);
   int per_sm = 1;
-  const int r = kernel_blocks(kern, kPairThreads, dyn, &per_sm);
+  const int r = kernel_blocks(reinterpret_cast<const void *>(sigma_pair_kernel), kPairThreads, 0, &per_sm);
   if (r != DOCI_OK) return r;
   int grid = sms * per_sm;
   if (grid > h->npblocks) grid = h->npblocks;
-  const uint2 *blocks = reinterpret_cast<const uint2 *>(h->d_pblocks);
-  const float *ks = reinterpret_cast<const float *>(h->d_kfrag);
-  if (lean)
-    sigma_pair_kernel<true><<<grid, kPairThreads, 0, st>>>(s, blocks, h->d_rowstart, h->d_binom, ks, h->d_ins,
-                                                           h->d_tab_off, x, y);
-  else
-    sigma_pair_kernel<false><<<grid, kPairThreads, dyn, st>>>(s, blocks, h->d_rowstart, h->d_binom, ks, h->d_ins,
-                                                              h->d_tab_off, x, y);
+  sigma_pair_kernel<<<grid, kPairThreads, 0, st>>>(s, reinterpret_cast<const uint2 *>(h->d_pblocks), h->d_rowstart,
+                                                   h->d_binom, reinterpret_cast<const float *>(h->d_kfrag), h->d_ins,
+                                                   h->d_tab_off, x, y);
   DOCI_CUDA(cudaGetLastError());
   return DOCI_OK;
 }

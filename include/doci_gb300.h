@@ -170,17 +170,23 @@ int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *s
 int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int64_t ldy, int nv, int precision,
                      void *stream);
 
-/* Sigma kernel selection for a handle: 0 automatic (default: with a row
- * tiling, kind 3 for FP32 and kind 4 for FP64, the fastest measured; else
- * kind 1), 1 the per-determinant gather kernel, 2 the row pass plus a
- * column-panel pass for the row-part hops, 3 the row pass alone doing all
- * hops, 4 the phase-ordered row pass (cross hops staged one source row at a
- * time), 5 kind 4 plus the column-panel pass, 6 the (N-1)-pair form (FP32
- * only: gather the L neighbours of every (N-1)-pair set, multiply by K on the
- * tensor cores, scatter-add; atomic adds, so the last bits vary between
- * runs; FP64 requests use the automatic choice), 7 the pair form with the
- * own row's sums in shared memory (slower; for comparison).  2-7 fall back
- * to 1 when the handle has no row tiling.  For tests and tuning. */
+/* Sigma kernel selection for a handle: 0 automatic (default: for FP32 on an
+ * sm_103a device with a row tiling that gives every SM work, kind 8; else
+ * with a row tiling kind 3 for FP32 and kind 4 for FP64; else kind 1),
+ * 1 the per-determinant gather kernel, 3 the row pass doing all hops, 4 the
+ * phase-ordered row pass (cross hops staged one source row at a time), 6 the
+ * (N-1)-pair form on the warp-level tensor-core path (FP32 only: gather the
+ * neighbours of every (N-1)-pair set, multiply by K, scatter with atomic
+ * adds), 8 the (N-1)-pair form on the 5th-generation tensor cores (FP32
+ * only: the own row of a set's row part staged in shared memory, the other
+ * rows streamed by TMA, the product in TMEM, each own row written once;
+ * needs a 16-byte aligned x, else kind 6 runs).  Kinds 6 and 8 reduce into
+ * sigma with atomic adds, so their last bits vary between runs; FP64
+ * requests for them use the automatic choice.  3-8 fall back to 1 when the
+ * handle has no row tiling.  Other values: DOCI_ERR_INVALID.  A device wait
+ * of kind 8 that runs out (it never should) is reported as
+ * DOCI_ERR_DEVICE_TIMEOUT by the handle's next synchronous call
+ * (doci_sigma_host, doci_solve).  For tests and tuning. */
 int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
 
 /* Autotuning: time the sigma paths that fit this handle's shape and keep
@@ -197,7 +203,7 @@ int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
 int doci_ham_autotune(doci_ham *ham, int precision, int nvec, int *choice);
 
 /* The path doci_sigma takes for this handle and precision: *kind as in
- * doci_ham_set_sigma_kernel (1..6; the automatic choice resolved) and
+ * doci_ham_set_sigma_kernel (1, 3, 4, 6 or 8; the automatic choice resolved) and
  * *launches, the number of kernel launches of one call.  Host-only query. */
 int doci_sigma_plan(const doci_ham *ham, int precision, int *kind, int *launches);
 

@@ -82,3 +82,31 @@ def test_pair_form_ranks(pair_exe, L, N, split, bs, ss):
     r = subprocess.run([pair_exe, str(L), str(N), str(split), str(bs), str(ss)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad=0" in r.stdout
+
+
+TC_SRC = os.path.join(HERE, "host_checks", "tc_check.cu")
+
+
+@pytest.fixture(scope="module")
+def tc_exe(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    out = str(tmp_path_factory.mktemp("tcc") / "tc_check")
+    subprocess.run([nvcc, "-O2", "-std=c++17", TC_SRC, "-o", out], check=True)
+    return out
+
+
+@pytest.mark.parametrize("L,N,split,us,ss", [
+    # whole spaces: every determinant reached once per pair it holds, its diagonal written once
+    (10, 5, 6, 1, 1), (12, 6, 8, 1, 1), (12, 3, 8, 1, 1), (12, 11, 8, 1, 1), (14, 7, 9, 1, 1),
+    (16, 8, 10, 1, 1), (18, 9, 9, 1, 1), (20, 10, 9, 1, 1), (9, 0, 8, 1, 1), (9, 9, 8, 1, 1),
+    (17, 1, 16, 1, 1), (17, 16, 16, 1, 1), (22, 11, 11, 1, 1), (24, 12, 16, 1, 1), (6, 6, 6, 1, 1),
+    (7, 0, 7, 1, 1), (32, 2, 16, 1, 1), (32, 30, 16, 1, 1),
+    # sampled large spaces: every index in range and equal to the direct rank
+    (32, 16, 16, 37, 101), (28, 14, 16, 11, 31), (30, 15, 16, 13, 7),
+])
+def test_tc_pair_form_ranks(tc_exe, L, N, split, us, ss):
+    r = subprocess.run([tc_exe, str(L), str(N), str(split), str(us), str(ss)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad=0" in r.stdout

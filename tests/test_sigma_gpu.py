@@ -50,7 +50,7 @@ def test_golden_sigma_diag_bits(name, fcidump, dg):
         assert np.array_equal(ranks.cpu().numpy(), np.arange(h.D))
 
 
-@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair", "pairsmem"])
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row1", "rowx", "pair", "tc"])
 @pytest.mark.parametrize("L,N,seed", [(16, 8, 21), (18, 5, 22), (20, 10, 23), (12, 1, 24), (12, 11, 25),
                                       (7, 0, 26), (6, 6, 27), (32, 2, 28), (32, 30, 29), (24, 12, 30),
                                       (22, 11, 31), (26, 4, 32)])
@@ -91,7 +91,7 @@ def test_addressing_full_size_properties(synth, dg):
             assert all(bin(int(v)).count("1") == 16 for v in b[:64])
 
 
-@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair", "pairsmem"])
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row1", "rowx", "pair", "tc"])
 def test_sigma_full_size_symmetry_and_linearity(kernel, synth, dg):
     """L=28, N=14 (D = 40,116,600): H is symmetric, sigma is linear, and
     sampled rows agree with the oracle's gather form."""
@@ -126,7 +126,7 @@ def test_sigma_full_size_symmetry_and_linearity(kernel, synth, dg):
         assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("kernel", ["auto", "gather", "row", "row1", "rowx", "rowxc", "pair", "pairsmem"])
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row1", "rowx", "pair", "tc"])
 def test_sigma_L32_fp32_vs_oracle_samples(kernel, synth, dg):
     """L=32, N=16 (D = 601,080,390), FP32: sampled rank windows across the
     whole space (start, middle, end) against the FP64 oracle gather form."""
@@ -190,7 +190,7 @@ def test_default_stream_orders_after_caller_work(synth, dg):
     p = synth(28, 14, 2)
     with dg.Hamiltonian.from_fcidump(p) as h:
         outs = []
-        for kernel in ("gather", "row"):
+        for kernel in ("gather", "row1", "tc"):
             h.set_sigma_kernel(kernel)
             g = torch.Generator(device="cuda").manual_seed(9)
             x = torch.randn(h.D, dtype=torch.float32, device="cuda", generator=g)
@@ -198,7 +198,8 @@ def test_default_stream_orders_after_caller_work(synth, dg):
             h.sigma_device(x.data_ptr(), y.data_ptr(), dg.FP32)
             outs.append(y)
         torch.cuda.synchronize()
-        assert (outs[0] - outs[1]).abs().max().item() <= 2e-6 * outs[0].abs().max().item()
+        for o in outs[1:]:
+            assert (outs[0] - o).abs().max().item() <= 2e-6 * outs[0].abs().max().item()
 
 
 @pytest.mark.parametrize("kernel", ["auto", "gather", "row1"])
@@ -241,18 +242,25 @@ def test_sigma_block_vs_oracle(L, N, seed, nv, kernel, synth, dg):
 
 def test_sigma_plan(synth, dg):
     """doci_sigma_plan reports the path doci_sigma takes: the automatic choice
-    resolves to the pair form (2 launches) for FP32 and the phase-ordered row
-    pass for FP64 once the tilings give every SM work, the gather kernel on
-    small spaces; an explicit kind is honoured."""
+    resolves to the tensor-core pair form for FP32 (one launch for the rows
+    without column elements and one per row-part size of the (N-1)-pair sets:
+    11 at L=20, N=10, split 9) and the phase-ordered row pass for FP64 once
+    the tilings give every SM work, the gather kernel on small spaces; an
+    explicit kind is honoured, FP32-only kinds fall back for FP64, and the
+    removed kinds are refused."""
     with dg.Hamiltonian.from_fcidump(synth(20, 10, 51)) as h:
-        assert h.sigma_plan(dg.FP32) == (6, 2)
+        assert h.sigma_plan(dg.FP32) == (8, 11)
         assert h.sigma_plan(dg.FP64) == (4, 1)
         h.set_sigma_kernel("row1")
         assert h.sigma_plan(dg.FP32) == (3, 1)
-        h.set_sigma_kernel("rowxc")
-        assert h.sigma_plan(dg.FP64) == (5, 2)
         h.set_sigma_kernel("pair")
+        assert h.sigma_plan(dg.FP32) == (6, 2)
         assert h.sigma_plan(dg.FP64) == (4, 1)  # FP32 only
+        h.set_sigma_kernel("tc")
+        assert h.sigma_plan(dg.FP64) == (4, 1)
+        for bad in (2, 5, 7, 9, -1):
+            with pytest.raises(dg.DociError):
+                h.set_sigma_kernel(bad)
     with dg.Hamiltonian.from_fcidump(synth(12, 6, 52)) as h:
         assert h.sigma_plan(dg.FP32) == (1, 1)
         assert h.sigma_plan(dg.FP64) == (1, 1)
