@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge measurement")
     ap.add_argument("--converge-repeats", type=int, default=20,
                     help="mixed solves of the L=28 N=14 Hamiltonian for time-to-converge p50/p99 (0 = none)")
-    ap.add_argument("--workload", choices=["sigma", "batch", "serve", "solve"], default="sigma",
+    ap.add_argument("--workload", choices=["sigma", "batch", "serve", "solve", "config2"], default="sigma",
                     help="sigma: the headline sigma benchmark; batch: many Hamiltonians, several roots; "
                          "serve: Poisson request stream through the request server")
     ap.add_argument("--problems", type=int, default=256, help="batch: number of Hamiltonians")
@@ -416,6 +416,42 @@ def solve_workload(a):
     print(json.dumps(line), flush=True)
 
 
+def config2_workload(a):
+    """The plain FP64 GPU Davidson (DAVIDSON_MAX_VEC 30, DAVIDSON_KEEP 2, TOL
+    1e-8, HF start) and CGP (MAX_ITS 40) on the L=28, N=14 Hamiltonian (seed
+    2), wall time from a built Hamiltonian, beside the reference executable's
+    wall times for the same runs recorded in tests/golden/golden.json (its
+    host and thread count stated there)."""
+    import doci_gb300 as dg
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+        gold = json.load(f)["cases"]["synthetic_L28_N14_s2"]
+    path = workload_path(28, 14, 2, 0, 1)
+    t0 = time.perf_counter()
+    with dg.Hamiltonian.from_fcidump(path) as h:
+        t_build = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        rd, _ = h.solve(solver="D", tol=1e-8, max_its=1000, davidson_max_vec=30, davidson_keep=2, mode="fp64")
+        t_d = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        rc, _ = h.solve(solver="CGP", tol=1e-8, max_its=40)
+        t_c = time.perf_counter() - t0
+    ref_d, ref_c = gold["D_exe"], gold["CGP_exe"]
+    line = {"metric": "FP64 Davidson / CGP solve wall time, L=28 N=14", "unit": "s", "higher_is_better": False,
+            "impl": "ours", "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+            "davidson": {"gpu_s": round(t_d, 3), "iterations": rd["iterations"], "energy": rd["energy"],
+                         "sigma_s": round(rd.get("sigma_seconds", 0.0), 3),
+                         "reference_s": ref_d["wall_s"], "reference_iterations": len(ref_d["trace"]),
+                         "reference_energy": ref_d["energy_printed"],
+                         "speedup": round(ref_d["wall_s"] / t_d, 1)},
+            "cgp": {"gpu_s": round(t_c, 3), "iterations": rc["iterations"], "energy": rc["energy"],
+                    "reference_s": ref_c["wall_s"], "reference_iterations": len(ref_c["trace"]) - 1,
+                    "reference_energy": ref_c["energy_printed"], "speedup": round(ref_c["wall_s"] / t_c, 1)},
+            "reference_host": gold["host"], "build_s": round(t_build, 2),
+            "config": {"workload": "DOCI L=28 N=14 D=40116600 seed=2, Davidson MAX_VEC 30 KEEP 2 TOL 1e-8; "
+                                   "CGP MAX_ITS 40"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
     ws, rank, local = dist_env()
@@ -427,6 +463,8 @@ def main():
         return serve_workload(a)
     if a.workload == "solve":
         return solve_workload(a)
+    if a.workload == "config2":
+        return config2_workload(a)
     import numpy as np
     import torch
     import doci_gb300 as dg

@@ -799,12 +799,12 @@ SigmaPlan plan_kind(const doci_ham *h, int precision, bool allow_pair, int kind)
   const size_t elem = precision == DOCI_FP64 ? 8 : 4;
   if (precision == DOCI_FP64 && (kind == 6 || kind == 8)) kind = 0;  // FP32-only forms: the automatic FP64 path
   if (allow_pair && precision == DOCI_FP32) {
-    // tensor-core pair form: the automatic FP32 choice where it fits and the
-    // space gives every SM units of work (measured fastest there)
-    const bool want_tc = kind == 8 || (kind == 0 && h->npblocks >= device_sm_count());
-    if (want_tc && tc_fits(h)) return {8, tc_launches(h)};
-    // mma.sync pair form: on request (kind 6)
-    if (kind == 6 && pair_fits(h)) return {6, 2};  // init pass + pair pass
+    // tensor-core pair form with TMA-staged hole rows: on request (kind 8)
+    if (kind == 8 && tc_fits(h)) return {8, tc_launches(h)};
+    // mma.sync pair form: the automatic FP32 choice where it fits and the
+    // space gives every SM blocks of work (measured fastest there)
+    const bool want_pair = kind == 6 || kind == 8 || (kind == 0 && h->npblocks >= device_sm_count());
+    if (want_pair && pair_fits(h)) return {6, 2};  // init pass + pair pass
   }
   // row kernel when the row tiling exists, fits, and gives every SM work
   bool row = kind >= 3 || (kind == 0 && h->nrows >= device_sm_count());
@@ -821,6 +821,7 @@ SigmaPlan plan_kind(const doci_ham *h, int precision, bool allow_pair, int kind)
 
 SigmaPlan plan_sigma(const doci_ham *h, int precision, bool allow_pair) {
   int kind = h->sigma_kernel;
+  if (precision == DOCI_FP64 && (kind == 6 || kind == 8)) kind = 0;  // FP32-only forms: the automatic FP64 path
   if (kind == 0) kind = tuned_choice(h, precision, 1, allow_pair);  // a tuned shape: its measured best
   return plan_kind(h, precision, allow_pair, kind);
 }

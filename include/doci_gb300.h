@@ -170,9 +170,9 @@ int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *s
 int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int64_t ldy, int nv, int precision,
                      void *stream);
 
-/* Sigma kernel selection for a handle: 0 automatic (default: for FP32 on an
- * sm_103a device with a row tiling that gives every SM work, kind 8; else
- * with a row tiling kind 3 for FP32 and kind 4 for FP64; else kind 1),
+/* Sigma kernel selection for a handle: 0 automatic (default: for FP32 with a
+ * row tiling that gives every SM work, kind 6; else with a row tiling kind 3
+ * for FP32 and kind 4 for FP64; else kind 1),
  * 1 the per-determinant gather kernel, 3 the row pass doing all hops, 4 the
  * phase-ordered row pass (cross hops staged one source row at a time), 6 the
  * (N-1)-pair form on the warp-level tensor-core path (FP32 only: gather the

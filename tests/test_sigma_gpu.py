@@ -242,22 +242,25 @@ def test_sigma_block_vs_oracle(L, N, seed, nv, kernel, synth, dg):
 
 def test_sigma_plan(synth, dg):
     """doci_sigma_plan reports the path doci_sigma takes: the automatic choice
-    resolves to the tensor-core pair form for FP32 (one launch for the rows
-    without column elements and one per row-part size of the (N-1)-pair sets:
-    11 at L=20, N=10, split 9) and the phase-ordered row pass for FP64 once
-    the tilings give every SM work, the gather kernel on small spaces; an
-    explicit kind is honoured, FP32-only kinds fall back for FP64, and the
-    removed kinds are refused."""
+    resolves to the mma.sync pair form for FP32 (a diag * x pass and the pair
+    pass) once the tiling gives every SM work, to a row pass for FP64 (or
+    the shape's tuned choice), the gather kernel on small spaces; an explicit
+    kind is honoured (the tensor-core pair form: one launch for the rows
+    without column elements and one per row-part size of the (N-1)-pair sets,
+    11 at L=20, N=10, split 9), FP32-only kinds take the automatic FP64 path,
+    and the removed kinds are refused."""
     with dg.Hamiltonian.from_fcidump(synth(20, 10, 51)) as h:
-        assert h.sigma_plan(dg.FP32) == (8, 11)
-        assert h.sigma_plan(dg.FP64) == (4, 1)
+        assert h.sigma_plan(dg.FP32) == (6, 2)
+        auto64 = h.sigma_plan(dg.FP64)
+        assert auto64[0] in (1, 3, 4)
         h.set_sigma_kernel("row1")
         assert h.sigma_plan(dg.FP32) == (3, 1)
         h.set_sigma_kernel("pair")
         assert h.sigma_plan(dg.FP32) == (6, 2)
-        assert h.sigma_plan(dg.FP64) == (4, 1)  # FP32 only
+        assert h.sigma_plan(dg.FP64) == auto64  # FP32 only
         h.set_sigma_kernel("tc")
-        assert h.sigma_plan(dg.FP64) == (4, 1)
+        assert h.sigma_plan(dg.FP32) == (8, 11)
+        assert h.sigma_plan(dg.FP64) == auto64
         for bad in (2, 5, 7, 9, -1):
             with pytest.raises(dg.DociError):
                 h.set_sigma_kernel(bad)
