@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--N", type=int, default=16)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
-    ap.add_argument("--kernel", choices=["auto", "gather", "row1", "rowx", "pair", "tc"], default="auto")
+    ap.add_argument("--kernel", choices=["auto", "gather", "row1", "rowx", "pair", "tc", "rowff"], default="auto")
     ap.add_argument("--block", type=int, default=1,
                     help="sigma: vectors per step through doci_sigma_block (1 = doci_sigma)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--sequential-sample", type=int, default=64, help="batch: one-at-a-time baseline sample")
     ap.add_argument("--roots", type=int, default=4)
     ap.add_argument("--workers", type=int, default=16)
-    ap.add_argument("--requests", type=int, default=200, help="serve: number of requests")
+    ap.add_argument("--requests", type=int, default=2000, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate, requests/s")
     ap.add_argument("--lmin", type=int, default=None)
     ap.add_argument("--lmax", type=int, default=None)
@@ -193,10 +193,11 @@ def converge_report(h, max_vec: int, mixed_tol: float, threshold: float = 1e-8):
     the mixed FP32/FP64 Davidson.  Only FP64-phase iterations of the mixed
     solve count (their energy is an FP64 Rayleigh quotient)."""
     import numpy as np
-    common = dict(solver="D", davidson_max_vec=max_vec, davidson_keep=2, max_its=200)
-    r64, _, t64 = h.solve_trace(tol=1e-7, mode="fp64", **common)
+    common = dict(solver="D", davidson_max_vec=max_vec, davidson_keep=2)
+    # E_FP64: the plain FP64 Davidson converged to a residual of 1e-10
+    r64, _, t64 = h.solve_trace(tol=1e-10, mode="fp64", max_its=400, **common)
     e_ref = r64["energy"]
-    rmx, _, tmx = h.solve_trace(tol=1e-7, mode="mixed", mixed_tol=mixed_tol, **common)
+    rmx, _, tmx = h.solve_trace(tol=1e-7, mode="mixed", mixed_tol=mixed_tol, max_its=200, **common)
 
     def first_time(tr, phase_ok):
         for ph, res, e, t in tr:
@@ -213,7 +214,7 @@ def converge_report(h, max_vec: int, mixed_tol: float, threshold: float = 1e-8):
             "dE_mixed_final": abs(rmx["energy"] - e_ref),
             "fp64_iterations_total": r64["iterations"], "mixed_iterations_fp32": rmx["iterations_fp32"],
             "mixed_iterations_fp64": rmx["iterations"] - rmx["iterations_fp32"],
-            "fp64_residual_final": r64["residual"], "max_vec": max_vec, "mixed_tol": mixed_tol,
+            "fp64_residual_final": r64["residual"], "fp64_tol": 1e-10, "max_vec": max_vec, "mixed_tol": mixed_tol,
             "note": "wall time from a built Hamiltonian (integrals, tables, diagonal on the device)"}
 
 
@@ -225,9 +226,9 @@ def converge_repeats(L: int, N: int, seed: int, repeats: int, max_vec: int, mixe
     solve of the same Hamiltonian."""
     import numpy as np
     import doci_gb300 as dg
-    common = dict(solver="D", davidson_max_vec=max_vec, davidson_keep=2, max_its=300)
+    common = dict(solver="D", davidson_max_vec=max_vec, davidson_keep=2, max_its=400)
     with dg.Hamiltonian.from_fcidump(workload_path(L, N, seed, 0, 1)) as h:
-        r64, _, t64 = h.solve_trace(tol=1e-7, mode="fp64", **common)
+        r64, _, t64 = h.solve_trace(tol=1e-10, mode="fp64", **common)
         e_ref = r64["energy"]
         hit64 = next((float(t) for ph, _, e, t in t64 if abs(e - e_ref) < threshold), None)
         times, dEs = [], []
@@ -355,48 +356,81 @@ def batch_workload(a):
 
 
 def serve_workload(a):
-    """Poisson request stream into the request server: per-request seeded
-    integrals, L uniform in [lmin, lmax], N = L // 2 + d, d uniform in -2..2."""
+    """Poisson request stream into the request server (continuous batching):
+    per-request seeded integrals, L uniform in [lmin, lmax], N = L // 2 + d,
+    d uniform in -2..2, mixed precision to a residual of 1e-6.  Reported:
+    solves/s over the stream, p50/p99 latency (queued to done), the server's
+    concurrency, and, on a sample of the same requests spread over the
+    stream: one-at-a-time solves/s (one worker, each request waited for) and
+    |E - E_FP64| against an independent plain FP64 Davidson solve of the
+    request (residual 1e-8)."""
     import numpy as np
     import doci_gb300 as dg
     from doci_gb300.fcidump import raw_integrals
-    lmin, lmax = a.lmin or 16, a.lmax or 24
+    lmin, lmax = a.lmin or 16, a.lmax or 30
     rng = np.random.default_rng(7)
     gaps = rng.exponential(1.0 / a.rate, size=a.requests)
-    reqs = []
+    shapes = []
     for i in range(a.requests):
         L = int(rng.integers(lmin, lmax + 1))
         N = max(1, min(L - 1, L // 2 + int(rng.integers(-2, 3))))
-        one, two = raw_integrals(L, 2000 + i)
-        reqs.append((L, N, one, two))
-    tickets = []
-    with dg.Server(nroots=1, tol=1e-5, mode="mixed", mixed_tol=1e-3, workers=a.workers) as srv:
+        shapes.append((L, N))
+    opts = dict(nroots=1, tol=1e-6, mode="mixed", mixed_tol=1e-3, max_its=400)
+    ints = [raw_integrals(L, 2000 + i) for i, (L, N) in enumerate(shapes)]  # made before the stream starts
+    tickets, conc = [], []
+    with dg.Server(workers=a.workers, **opts) as srv:
         t0 = time.perf_counter()
         at = 0.0
-        for (L, N, one, two), g in zip(reqs, gaps):
+        for i, ((L, N), g) in enumerate(zip(shapes, gaps)):
             at += g
+            one, two = ints[i]
             wait = at - (time.perf_counter() - t0)
             if wait > 0:
                 time.sleep(wait)
             tickets.append(srv.submit(L, N, one, two))
+            conc.append(srv.stats()["running"])
         res = [srv.wait(t) for t in tickets]
         span = time.perf_counter() - t0
     lat = [r["end_s"] - r["queued_s"] for r in res]
-    dE = [abs(r["energies_fp32"][0] - r["energies"][0]) for r in res]
+    del tickets
+    # sample of the stream for the one-at-a-time and FP64 comparisons
+    k = min(a.sequential_sample, a.requests)
+    idx = np.linspace(0, a.requests - 1, k).astype(int)
+    t_seq = 0.0
+    with dg.Server(workers=1, **opts) as one_srv:
+        for i in idx:
+            L, N = shapes[i]
+            one, two = ints[i]
+            t1 = time.perf_counter()
+            one_srv.wait(one_srv.submit(L, N, one, two))
+            t_seq += time.perf_counter() - t1
+    dE, dE_by_L = [], {}
+    for i in idx:
+        L, N = shapes[i]
+        one, two = ints[i]
+        with dg.Hamiltonian.from_integrals(L, N, 0.0, one, two) as h:
+            r64, _ = h.solve(solver="D", tol=1e-8, max_its=1000, davidson_max_vec=30, davidson_keep=2, mode="fp64")
+        d = abs(res[i]["energies"][0] - r64["energy"])
+        dE.append(d)
+        dE_by_L[L] = max(dE_by_L.get(L, 0.0), d)
     line = {"metric": "serving p50/p99 latency and solves/s (Poisson arrivals)", "value": round(a.requests / span, 3),
             "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "impl": "ours", "dtype": "f32+f64",
             "data": "synthetic", "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99),
-            "offered_rate": a.rate, "requests": a.requests,
+            "max_latency_s": max(lat), "span_s": round(span, 2), "offered_rate": a.rate, "requests": a.requests,
             "ok": int(sum(r["status"] == 0 for r in res)), "converged": int(sum(r["converged"] for r in res)),
-            "fp32_phase_dE_max_Ha": max(dE) if dE else None,
-            "note": "final energies are FP64-refined (FP64 block-Davidson phase to tol); fp32_phase_dE is "
-                    "|E(FP32 phase) - E(final)| per request",
+            "residual_max": max(r["residuals"][0] for r in res),
+            "running_at_submit": {"p50": pct(conc, 50), "max": max(conc)},
+            "one_at_a_time": {"solves_per_s": round(k / t_seq, 3), "sample": k},
+            "speedup_vs_one_at_a_time": round((a.requests / span) / (k / t_seq), 3),
+            "dE_vs_fp64": {"max_Ha": max(dE), "median_Ha": pct(dE, 50), "sample": k,
+                           "max_by_L": {str(L): v for L, v in sorted(dE_by_L.items())},
+                           "reference": "independent plain FP64 Davidson of the same request, residual 1e-8"},
             "config": {"workload": f"{a.requests} requests, L uniform in {lmin}..{lmax}, N=L//2+-2, "
-                                   f"rate {a.rate}/s, workers={a.workers}"}}
+                                   f"Poisson {a.rate}/s, workers={a.workers}", "opts": opts}}
     print(json.dumps(line), flush=True)
 
 
-KERNEL_NAMES = {1: "gather", 3: "row1", 4: "rowx", 6: "pair", 8: "tc"}
+KERNEL_NAMES = {1: "gather", 3: "row1", 4: "rowx", 6: "pair", 8: "tc", 9: "rowff"}
 
 
 def solve_workload(a):

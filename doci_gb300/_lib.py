@@ -168,7 +168,7 @@ def default_opts(**kw) -> SolveOpts:
     return o
 
 
-KERNEL_KINDS = {"auto": 0, "gather": 1, "row1": 3, "rowx": 4, "pair": 6, "tc": 8}
+KERNEL_KINDS = {"auto": 0, "gather": 1, "row1": 3, "rowx": 4, "pair": 6, "tc": 8, "rowff": 9}
 KERNEL_NAMES = {v: k for k, v in KERNEL_KINDS.items()}
 
 
@@ -222,7 +222,8 @@ class Hamiltonian:
 
     def set_sigma_kernel(self, kind) -> None:
         """0/'auto', 1/'gather', 3/'row1' (row pass), 4/'rowx' (phase-ordered row pass),
-        6/'pair' (pair form, mma.sync), 8/'tc' (pair form, tcgen05); doci_ham_set_sigma_kernel."""
+        6/'pair' (pair form, mma.sync), 8/'tc' (pair form, tcgen05), 9/'rowff' (FP64 float-float row
+        pass); doci_ham_set_sigma_kernel."""
         kind = KERNEL_KINDS.get(kind, kind)
         _check(lib().doci_ham_set_sigma_kernel(self._h, int(kind)), "doci_ham_set_sigma_kernel")
 

@@ -185,10 +185,15 @@ struct doci_server {
   std::vector<std::thread> workers;
   int64_t next_ticket = 1, in_use = 0, running = 0, submitted = 0, finished = 0;
   bool stop = false;
+  int device = 0;  // the device current when the server was created: every worker solves on it
 
   void worker_main() {
-    cudaStream_t st;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return;
+    cudaStream_t st = nullptr;
+    // a worker without its device or stream still takes requests and completes
+    // them with DOCI_ERR_CUDA, so that no ticket stays pending
+    bool usable = cudaSetDevice(device) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    if (!usable) cudaGetLastError();
     for (;;) {
       Req r;
       {
@@ -201,7 +206,7 @@ struct doci_server {
       doci_root_result res;
       std::memset(&res, 0, sizeof res);
       res.queued_s = r.queued;
-      res.status = run(r, st, &res);
+      res.status = usable ? run(r, st, &res) : DOCI_ERR_CUDA;
       res.end_s = clock_s() - t0;
       {
         std::lock_guard<std::mutex> lk(mu);
@@ -210,7 +215,7 @@ struct doci_server {
       }
       cv_done.notify_all();
     }
-    cudaStreamDestroy(st);
+    if (st) cudaStreamDestroy(st);
   }
 
   int run(Req &r, cudaStream_t st, doci_root_result *res) {
@@ -323,6 +328,11 @@ int doci_server_create(const doci_batch_opts *opts, doci_server **out) {
   if (!srv) return DOCI_ERR_OUT_OF_MEMORY;
   if (opts) srv->opts = *opts; else doci_batch_opts_default(&srv->opts);
   if (srv->opts.workers < 1) srv->opts.workers = 1;
+  if (cudaGetDevice(&srv->device) != cudaSuccess) {
+    cudaGetLastError();
+    delete srv;
+    return DOCI_ERR_NO_DEVICE;
+  }
   srv->budget = srv->opts.hbm_budget;
   if (srv->budget <= 0) {
     size_t fr = 0, tot = 0;

@@ -276,7 +276,8 @@ int doci_ham_autotune(doci_ham *h, int precision, int nvec, int *choice) {
 }
 
 int doci_ham_set_sigma_kernel(doci_ham *h, int kind) {
-  if (!h || !(kind == 0 || kind == 1 || kind == 3 || kind == 4 || kind == 6 || kind == 8)) return DOCI_ERR_INVALID;
+  if (!h || !(kind == 0 || kind == 1 || kind == 3 || kind == 4 || kind == 6 || kind == 8 || kind == 9))
+    return DOCI_ERR_INVALID;
   h->sigma_kernel = kind;
   return DOCI_OK;
 }
@@ -290,8 +291,11 @@ int doci_sigma_host(doci_ham *h, const void *x, void *y, int precision) {
   // pinned host buffers are read and written by copy kernels through their
   // device mapping (all SMs on the host link, faster than one copy engine);
   // pageable ones go through cudaMemcpyAsync
-  const void *dx = mapped_host(x);
-  void *dy = const_cast<void *>(mapped_host(y));
+  // (the copy kernels move 4-byte words: a pinned buffer that is not 4-byte
+  // aligned takes the cudaMemcpyAsync path too)
+  const bool words = (reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) % 4 == 0;
+  const void *dx = words ? mapped_host(x) : nullptr;
+  void *dy = words ? const_cast<void *>(mapped_host(y)) : nullptr;
   if (dx) {
     if ((st = vec_copy(h->d_stage_x, dx, bytes, h->stream))) return st;
   } else {
@@ -325,14 +329,15 @@ int doci_multidot(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   double *partials = nullptr;
   DOCI_CUDA(cudaMallocAsync(&partials, sizeof(double) * vec_partials_capacity(), st));
-  if (const int si = vec_partials_init(partials, st)) return si;
-  int s = precision == DOCI_FP64
+  int s = vec_partials_init(partials, st);
+  if (s == DOCI_OK)
+    s = precision == DOCI_FP64
               ? vec_multidot<double>(static_cast<const double *>(d_V), static_cast<size_t>(ld), m,
                                      static_cast<const double *>(d_w), static_cast<size_t>(n), partials, st)
               : vec_multidot<float>(static_cast<const float *>(d_V), static_cast<size_t>(ld), m,
                                     static_cast<const float *>(d_w), static_cast<size_t>(n), partials, st, true);
   if (s == DOCI_OK) s = vec_reduce(partials, m, d_out, st);
-  const cudaError_t e = cudaFreeAsync(partials, st);
+  const cudaError_t e = cudaFreeAsync(partials, st);  // on every path after the allocation
   if (s != DOCI_OK) return s;
   DOCI_CUDA(e);
   return DOCI_OK;

@@ -37,7 +37,9 @@ std::mutex g_mu;
 double *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device, looked up once
-// per device (host code cannot use the symbol itself as a device pointer).
+// per device (host code cannot use the symbol itself as a device pointer) and
+// kept for the life of the process: a cudaDeviceReset reloads the device image
+// elsewhere, so the entry point is not for use on a device after a reset.
 int scratch_address(double **out) {
   int dev = 0;
   DOCI_CUDA(cudaGetDevice(&dev));

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "addressing.cuh"
+#include "ff.cuh"
 #include "internal.h"
 
 namespace doci {
@@ -618,13 +619,17 @@ __device__ __forceinline__ Real table_gather(const uint32_t *__restrict__ ent, i
   return a;
 }
 
+// Real: the arithmetic (double, float, or float-float with double tables,
+// diagonal and output and a float-float x: Io<Real>)
 template <typename Real, int NHB>
 __global__ void __launch_bounds__(kRowxThreads, 2)
 sigma_rowx_kernel(RowShape s, int with_across, uint32_t row_pad, const uint2 *__restrict__ rows,
                   const uint32_t *__restrict__ rowstart_of, const uint32_t *__restrict__ g_binom,
-                  const Real *__restrict__ g_K, const uint32_t *__restrict__ rem_tab,
+                  const typename Io<Real>::T *__restrict__ g_K, const uint32_t *__restrict__ rem_tab,
                   const uint32_t *__restrict__ ins_tab, const uint32_t *__restrict__ tab_off,
-                  const Real *__restrict__ diag, const Real *__restrict__ x, Real *__restrict__ y) {
+                  const typename Io<Real>::T *__restrict__ diag, const Real *__restrict__ x,
+                  typename Io<Real>::T *__restrict__ y) {
+  using IO = Io<Real>;
   __shared__ RowxTables<Real> tb;
   extern __shared__ __align__(16) unsigned char rowx_smem[];
   Real *acc = reinterpret_cast<Real *>(rowx_smem);
@@ -633,7 +638,7 @@ sigma_rowx_kernel(RowShape s, int with_across, uint32_t row_pad, const uint2 *__
   for (int t = threadIdx.x; t < 17 * kBinomCols; t += blockDim.x) tb.binom[t] = g_binom[t];
   for (int t = threadIdx.x; t < 256; t += blockDim.x) {
     const int m = t >> 4, q = t & 15;
-    tb.Kb[t] = (m < sp && q < sp) ? g_K[m * 32 + q] : Real(0);
+    tb.Kb[t] = (m < sp && q < sp) ? IO::in(g_K[m * 32 + q]) : Real(0);
   }
   const uint32_t *B = tb.binom;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -669,7 +674,7 @@ sigma_rowx_kernel(RowShape s, int with_across, uint32_t row_pad, const uint2 *__
         const int e = t / nhl, h = t % nhl;
         const int a_e = __fns(eb, 0, e + 1), a_h = __fns(hb, 0, h + 1);
         tb.aa_rs[t] = rowstart_of[(mask & ~(1u << a_e)) | (1u << a_h)];
-        tb.aa_K[t] = g_K[(sp + a_e) * 32 + sp + a_h];
+        tb.aa_K[t] = IO::in(g_K[(sp + a_e) * 32 + sp + a_h]);
       }
     }
     const uint32_t n = B[sp * kBinomCols + j];
@@ -688,16 +693,16 @@ sigma_rowx_kernel(RowShape s, int with_across, uint32_t row_pad, const uint2 *__
         Real a;
         __device__ __forceinline__ void begin(int m) { Krow = Kb + m * 16; }
         __device__ __forceinline__ void hop(int, int q, uint32_t cc) { a += Krow[q] * buf[cc]; }
-      } f{tb.Kb, buf, tb.Kb, diag[rstart + c] * buf[c]};
+      } f{tb.Kb, buf, tb.Kb, IO::in(diag[rstart + c]) * buf[c]};
       nb.visit(Mb, p, n - 1, j, sp - j, B, f);
       Real a2 = 0;
       int t = 0;
       for (; t + 4 <= n_aa; t += 4) {
-        const Real v0 = __ldg(x + tb.aa_rs[t] + c), v1 = __ldg(x + tb.aa_rs[t + 1] + c);
-        const Real v2 = __ldg(x + tb.aa_rs[t + 2] + c), v3 = __ldg(x + tb.aa_rs[t + 3] + c);
+        const Real v0 = ldg_val(x + tb.aa_rs[t] + c), v1 = ldg_val(x + tb.aa_rs[t + 1] + c);
+        const Real v2 = ldg_val(x + tb.aa_rs[t + 2] + c), v3 = ldg_val(x + tb.aa_rs[t + 3] + c);
         a2 += tb.aa_K[t] * v0 + tb.aa_K[t + 1] * v1 + tb.aa_K[t + 2] * v2 + tb.aa_K[t + 3] * v3;
       }
-      for (; t < n_aa; ++t) a2 += tb.aa_K[t] * __ldg(x + tb.aa_rs[t] + c);
+      for (; t < n_aa; ++t) a2 += tb.aa_K[t] * ldg_val(x + tb.aa_rs[t] + c);
       acc[c] = f.a + a2;
     }
     // column part -> row part: sources R u q, one at a time
@@ -706,7 +711,7 @@ sigma_rowx_kernel(RowShape s, int with_across, uint32_t row_pad, const uint2 *__
       const uint32_t *remj = rem_tab + tab_off[j];
       for (int t = 0; t < n_ba; ++t) {
         __syncthreads();
-        if (threadIdx.x < 16) tb.Kx[threadIdx.x] = threadIdx.x < sp ? g_K[threadIdx.x * 32 + tb.ba_q[t]] : Real(0);
+        if (threadIdx.x < 16) tb.Kx[threadIdx.x] = threadIdx.x < sp ? IO::in(g_K[threadIdx.x * 32 + tb.ba_q[t]]) : Real(0);
         stage_row(buf, x + tb.ba_rs[t], n_dn);
         __syncthreads();
         for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) acc[c] += table_gather(remj + 16 * c, j, tb.Kx, buf);
@@ -718,7 +723,7 @@ sigma_rowx_kernel(RowShape s, int with_across, uint32_t row_pad, const uint2 *__
       const uint32_t *insj = ins_tab + tab_off[j];
       for (int t = 0; t < n_ab; ++t) {
         __syncthreads();
-        if (threadIdx.x < 16) tb.Kx[threadIdx.x] = threadIdx.x < sp ? g_K[tb.ab_m[t] * 32 + threadIdx.x] : Real(0);
+        if (threadIdx.x < 16) tb.Kx[threadIdx.x] = threadIdx.x < sp ? IO::in(g_K[tb.ab_m[t] * 32 + threadIdx.x]) : Real(0);
         stage_row(buf, x + tb.ab_rs[t], n_up);
         __syncthreads();
         for (uint32_t c = threadIdx.x; c < n; c += blockDim.x)
@@ -726,7 +731,7 @@ sigma_rowx_kernel(RowShape s, int with_across, uint32_t row_pad, const uint2 *__
       }
     }
     __syncthreads();
-    for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) y[rstart + c] = acc[c];
+    for (uint32_t c = threadIdx.x; c < n; c += blockDim.x) y[rstart + c] = IO::out(acc[c]);
   }
 }
 
@@ -748,6 +753,40 @@ int launch_rowx(const doci_ham *h, const void *x, void *y, cudaStream_t st, int 
                                         h->d_rowstart, h->d_binom, K, h->d_rem, h->d_ins, h->d_tab_off, dg,
                                         static_cast<const Real *>(x), static_cast<Real *>(y));
   DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+unsigned grid_for(uint64_t n);
+
+__global__ void to_ff_kernel(const double *__restrict__ x, ff *__restrict__ out, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = ff_from(x[i]);
+}
+
+// FP64-accurate sigma in float-float arithmetic: x converted to float-float
+// once (stream-ordered scratch of D x 8 bytes), the phase-ordered row pass
+// on it, double diagonal and output
+int launch_rowx_ff(const doci_ham *h, const double *x, double *y, cudaStream_t st) {
+  const RowShape s{h->D, h->L, h->N, h->split, h->L - h->split, h->nrows};
+  const uint32_t pad = (static_cast<uint32_t>(h->max_row) + 3u) & ~3u;
+  const size_t dyn = 2 * static_cast<size_t>(pad) * sizeof(ff);
+  auto kern = sigma_rowx_kernel<ff, 16>;
+  int blocks_per_sm = 1;
+  DOCI_TRY_S(blocks_for(kern, kRowxThreads, dyn, &blocks_per_sm));
+  int grid = device_sm_count() * blocks_per_sm;
+  if (grid > h->nrows) grid = h->nrows;
+  ff *xf = nullptr;
+  DOCI_CUDA(cudaMallocAsync(&xf, sizeof(ff) * static_cast<size_t>(h->D), st));
+  to_ff_kernel<<<grid_for(h->D), kThreads, 0, st>>>(x, xf, h->D);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    kern<<<grid, kRowxThreads, dyn, st>>>(s, 1, pad, reinterpret_cast<const uint2 *>(h->d_rows), h->d_rowstart,
+                                          h->d_binom, h->d_Kmir64, h->d_rem, h->d_ins, h->d_tab_off, h->d_diag, xf,
+                                          y);
+    e = cudaGetLastError();
+  }
+  const cudaError_t ef = cudaFreeAsync(xf, st);
+  DOCI_CUDA(e);
+  DOCI_CUDA(ef);
   return DOCI_OK;
 }
 
@@ -806,6 +845,9 @@ SigmaPlan plan_kind(const doci_ham *h, int precision, bool allow_pair, int kind)
     const bool want_pair = kind == 6 || kind == 8 || (kind == 0 && h->npblocks >= device_sm_count());
     if (want_pair && pair_fits(h)) return {6, 2};  // init pass + pair pass
   }
+  // float-float phase-ordered row pass (FP64 accuracy in FP32 arithmetic):
+  // the x conversion and the row pass
+  if (kind == 9 && precision == DOCI_FP64 && h->nrows >= 1 && rowx_fits(h, sizeof(ff))) return {9, 2};
   // row kernel when the row tiling exists, fits, and gives every SM work
   bool row = kind >= 3 || (kind == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
@@ -822,6 +864,7 @@ SigmaPlan plan_kind(const doci_ham *h, int precision, bool allow_pair, int kind)
 SigmaPlan plan_sigma(const doci_ham *h, int precision, bool allow_pair) {
   int kind = h->sigma_kernel;
   if (precision == DOCI_FP64 && (kind == 6 || kind == 8)) kind = 0;  // FP32-only forms: the automatic FP64 path
+  if (precision == DOCI_FP32 && kind == 9) kind = 0;                 // FP64-only form: the automatic FP32 path
   if (kind == 0) kind = tuned_choice(h, precision, 1, allow_pair);  // a tuned shape: its measured best
   return plan_kind(h, precision, allow_pair, kind);
 }
@@ -854,6 +897,8 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
       return f64 ? launch_typed<double>(h, x, y, st) : launch_typed<float>(h, x, y, st);
     case 4:
       return f64 ? launch_rowx<double>(h, x, y, st, 1) : launch_rowx<float>(h, x, y, st, 1);
+    case 9:
+      return launch_rowx_ff(h, static_cast<const double *>(x), static_cast<double *>(y), st);
     default:  // 3
       return f64 ? launch_row<double>(h, x, y, st, 1) : launch_row<float>(h, x, y, st, 1);
   }
@@ -951,8 +996,9 @@ int autotune_sigma(doci_ham *h, int precision, int nv, cudaStream_t st, int *cho
     for (int allow = 0; allow < 2; ++allow) {
       double best_ms = 1e30;
       int pick = 0;
-      for (int kind : {1, 3, 4, 6, 8}) {
+      for (int kind : {1, 3, 4, 6, 8, 9}) {
         if ((kind == 6 || kind == 8) && (!allow || precision != DOCI_FP32)) continue;
+        if (kind == 9 && precision != DOCI_FP64) continue;
         hm->sigma_kernel = kind;
         const SigmaPlan p = plan_sigma(h, precision, allow != 0);
         if (p.kind != kind) continue;  // the path does not fit this shape

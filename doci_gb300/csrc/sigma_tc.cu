@@ -1,5 +1,6 @@
 // sigma_tc.cu -- FP32 sigma in the (N-1)-pair form on the 5th-generation
-// tensor cores (tcgen05.mma kind::tf32, TMEM accumulators, TMA bulk loads).
+// tensor cores (tcgen05.mma kind::tf32 with the A operand and the
+// accumulators in tensor memory, TMA bulk loads of the streamed rows).
 //
 // The Hamiltonian's off-diagonal elements are the pair hops T -> T \ i u a
 // with weight K_ia (doci.c:216-222, the hops prev_bitstring enumerates,
@@ -22,11 +23,14 @@
 //     consecutive elements, streamed with TMA bulk copies (x) and coalesced
 //     reductions (sigma).
 //
-// Per tile of 128 sets the 32-wide rows X_S (columns 0..15: the column-part
-// orbitals, 16..31: the unit's row-part holes) are split into TF32 high and
-// low parts in shared memory (128-byte swizzled, K-major) and multiplied by
-// the unit's 32 x 32 K (also split) with three tcgen05.mma passes
-// (lo*hi + hi*lo + hi*hi, FP32 accumulation in TMEM): FP32 accuracy.
+// Per tile of 128 sets (the MMA's M; one set per thread of a 4-warp group,
+// which is also the set's tensor-memory lane) the 32-wide rows X_S (columns
+// 0..15: the column-part orbitals, 16..31: the unit's row-part holes) are
+// split into TF32 high and low parts and stored straight into tensor memory
+// (tcgen05.st), where the MMA reads its A operand; the unit's 32 x 32 K
+// (also split) is the B operand in shared memory (128-byte swizzled,
+// K-major).  Three tcgen05.mma passes (hi*hi + hi*lo + lo*hi, FP32
+// accumulation in tensor memory) give FP32 accuracy.
 //
 // Ordering instead of atomics for the own rows: the units of one row-part
 // size kp run in one launch, launches go from the largest kp down.  Own row
@@ -36,14 +40,16 @@
 // first small launch.  So sigma needs no zero fill and each own row crosses
 // HBM once each way; the hole rows' reductions are the only read-modify-write
 // traffic.  The reduction order of the hole rows varies from run to run (the
-// result's last bits with it).
+// result's last bits with it).  Units run in colex order of their row part,
+// so the units resident at one time share many hole rows in L2.
 //
-// Warp roles of a block (one block per SM): warps 0-3 and 4-7 gather and
-// scatter alternate tiles, warp 8 issues the TMA loads of the hole rows,
-// warp 9 issues the MMAs.  All waits are bounded: a wait that runs out sets
-// the block's abort flag and the launch's error word, every role then leaves
-// its loop, in-flight copies and MMAs are drained (again bounded) and TMEM is
-// freed.
+// Warp roles of a block (one block per SM): warps 0-15 form four groups of
+// four that gather, split and scatter alternate tiles (four tiles in flight,
+// each with its own 96 columns of tensor memory), warp 16 issues the TMA
+// loads of the hole rows, warp 17 issues the MMAs.  All waits are bounded: a
+// wait that runs out sets the block's abort flag and the launch's error word,
+// every role then leaves its loop, in-flight copies and MMAs are drained
+// (again bounded) and the tensor memory is freed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -60,10 +66,15 @@
 namespace doci {
 namespace {
 
-constexpr int kTcThreads = 320;       // 10 warps
-constexpr int kTile = 128;            // sets per tile (the MMA's M)
-constexpr int kStages = 3;            // hole-row stages in flight
-constexpr int kSlot = 136;            // floats per hole segment slot (128 + alignment slack)
+constexpr int kGroups = 4;                       // tiles in flight
+constexpr int kGatherWarps = 4 * kGroups;        // warps 0-15
+constexpr int kProdWarp = kGatherWarps;          // warp 16: TMA producer
+constexpr int kMmaWarp = kGatherWarps + 1;       // warp 17: MMA issue
+constexpr int kTcThreads = 32 * (kGatherWarps + 2);
+constexpr int kTile = 128;                       // sets per tile (the MMA's M)
+constexpr int kStages = 6;                       // hole-row stages in flight
+constexpr int kSlot = 136;                       // floats per hole segment slot (128 + alignment slack)
+constexpr uint32_t kTmemCols = 512;              // per group: A hi 32 | A lo 32 | D 32 (stride 128)
 // tcgen05 instruction descriptor: D FP32 (bits 4-5 = 1), A and B TF32 (bits
 // 7-9, 10-12 = 2), both K-major, N = 32 (bits 17-22 = N >> 3), M = 128
 // (bits 24-28 = M >> 4)
@@ -82,16 +93,20 @@ struct TcShape {
 };
 
 // shared-memory layout (dynamic; the base is 1024-byte aligned)
-constexpr int kOffA = 0;                                     // [group][hi, lo] 16 KB each
-constexpr int kOffB = kOffA + 4 * 16384;                     // K: hi, lo 4 KB each
+constexpr int kOffB = 0;                                     // K: hi, lo 4 KB each (swizzled)
 constexpr int kOffStage = kOffB + 2 * 4096;                  // [stage][hole][kSlot] floats
 constexpr int kStageBytes = 16 * kSlot * 4;
 constexpr int kOffBar = kOffStage + kStages * kStageBytes;   // mbarriers (8 B each)
-constexpr int kNumBars = 2 * kStages + 2 + 2 + 1;            // hx_full, hx_empty, a_full, acc_full, drain
+constexpr int kNumBars = 2 * kStages + 2 * kGroups + 1;      // hx_full, hx_empty, a_full, acc_full, drain
 constexpr int kOffMisc = kOffBar + 8 * kNumBars;             // tmem slot, abort flag, hole rows / orbitals
 constexpr int kOffTables = kOffMisc + 16 + 2 * 16 * 4;       // c8 (256 B) then G
 constexpr int kTablesBytes = tc::kTablesBytes;
-constexpr int kOffRows = (kOffTables + kTablesBytes + 15) & ~15;  // x_own, then sigma_own
+constexpr int kOffCset = (kOffTables + kTablesBytes + 15) & ~15;  // this launch's column sets (u16)
+constexpr int kCsetMax = 12870;                              // C(16, 8)
+constexpr int kOffRows = (kOffCset + 2 * kCsetMax + 15) & ~15;    // x_own, then sigma_own
+// at least this much shared memory per block, so that one block runs per SM
+// (each block allocates all 512 tensor-memory columns)
+constexpr size_t kMinSmem = 120 * 1024;
 
 __host__ __device__ constexpr size_t tc_smem_bytes(uint32_t n_own) {
   return static_cast<size_t>(kOffRows) + 2 * ((static_cast<size_t>(n_own) * 4 + 15) & ~size_t(15));
@@ -129,6 +144,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, long limi
   atomicCAS(err, 0, code);
   return false;
 }
+// the same wait by every lane of a warp, with one verdict for the warp (the
+// .sync.aligned tensor-memory instructions that follow need the whole warp)
+__device__ __forceinline__ bool warp_wait(uint32_t a, uint32_t parity, long limit, volatile int *abort_flag, int *err,
+                                          int code) {
+  const bool r = mbar_wait(a, parity, limit, abort_flag, err, code);
+  return __all_sync(0xffffffffu, r);
+}
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
                "l"(src), "r"(bytes), "r"(bar)
@@ -144,15 +166,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
          (static_cast<uint64_t>(1024 >> 4) << 32) | (static_cast<uint64_t>(1) << 46) |
          (static_cast<uint64_t>(2) << 61);
 }
-__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t da, uint64_t db, uint32_t acc) {
+// D (tensor memory) [+]= A (tensor memory) x B (shared memory descriptor)
+__device__ __forceinline__ void tc_mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t db, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-      "l"(da), "l"(db), "r"(kIdesc), "r"(acc));
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(db), "r"(kIdesc), "r"(acc));
 }
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
+// 32 columns of this warp's 32 tensor-memory lanes, one lane per thread
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&y)[32]) {
   uint32_t r[32];
   asm volatile(
@@ -167,6 +191,17 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&y)[32]) {
 #pragma unroll
   for (int i = 0; i < 32; ++i) y[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]),
+      "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]),
+      "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ uint32_t tf32_rna(float f) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(f));
@@ -204,19 +239,21 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
   extern __shared__ __align__(1024) uint8_t sm[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t base = su32(sm);
-  if (base & 1023u) {  // the swizzled tiles need a 1024-byte aligned base
+  if (base & 1023u) {  // the swizzled K tiles need a 1024-byte aligned base
     if (tid == 0) atomicCAS(err, 0, 3);
     return;
   }
   uint64_t *bars = reinterpret_cast<uint64_t *>(sm + kOffBar);
   auto bar = [&](int i) { return su32(bars + i); };
-  const int B_HXF = 0, B_HXE = kStages, B_AF = 2 * kStages, B_ACC = 2 * kStages + 2, B_DRAIN = 2 * kStages + 4;
+  const int B_HXF = 0, B_HXE = kStages, B_AF = 2 * kStages, B_ACC = 2 * kStages + kGroups,
+            B_DRAIN = 2 * kStages + 2 * kGroups;
   uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + kOffMisc);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kOffMisc + 4);
   uint32_t *hole_rs = reinterpret_cast<uint32_t *>(sm + kOffMisc + 16);
   int *hole_orb = reinterpret_cast<int *>(sm + kOffMisc + 16 + 64);
-  uint8_t *c8 = sm + kOffTables;
-  uint16_t *Gt = reinterpret_cast<uint16_t *>(sm + kOffTables + 256);
+  const uint8_t *c8 = sm + kOffTables;
+  const uint16_t *Gt = reinterpret_cast<const uint16_t *>(sm + kOffTables + 256);
+  uint16_t *cs_sm = reinterpret_cast<uint16_t *>(sm + kOffCset);
   const size_t row_bytes = ((static_cast<size_t>(s.n_own) * 4 + 15) & ~size_t(15));
   float *x_own = reinterpret_cast<float *>(sm + kOffRows);
   float *s_own = reinterpret_cast<float *>(sm + kOffRows + row_bytes);
@@ -224,9 +261,11 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
 
   const int lo = s.lo, sp = s.sp, nhr = s.nhr;
   const bool has_own = s.n_own > 0;
+  const uint32_t Dl = s.D & ~3u;  // end of the vector's last whole 16-byte chunk
 
-  // tables: c8[P] (colex of the low part), G[Q][p]
+  // per-launch tables: c8[P] (colex of the low part), G[Q][p], the column sets
   for (int i = tid; i < kTablesBytes; i += kTcThreads) sm[kOffTables + i] = g_tables[i];
+  for (uint32_t i = tid; i < s.n_s; i += kTcThreads) cs_sm[i] = cset[s.cset_off + i];
   if (tid == 0) {
     for (int i = 0; i < kNumBars; ++i) {
       const uint32_t cnt = (i >= B_HXE && i < B_AF) ? 4u : (i >= B_AF && i < B_ACC) ? 4u : 1u;
@@ -235,8 +274,9 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 9) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(su32(tslot)));
+  if (warp == kMmaWarp) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)),
+                 "r"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -291,67 +331,71 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
     __syncthreads();
     tc_fence_after();
 
-    if (warp < 8 && ok) {
-      // ---- gather / MMA hand-off / scatter, tiles T with T & 1 == group
-      // group g takes the tiles T = T0 + t with T & 1 == g (the MMA warp's accumulator choice)
-      const int g = warp >> 2, gt = tid & 127;
-      for (uint32_t t = static_cast<uint32_t>(g) ^ (T0 & 1u); t < ntiles; t += 2) {
+    if (warp < kGatherWarps && ok) {
+      // ---- gather / split into tensor memory / MMA hand-off / scatter:
+      // group g takes the tiles T = T0 + t with T % 4 == g
+      const int g = warp >> 2, q = warp & 3, gt = 32 * q + lane;
+      const uint32_t t_grp = tmem + static_cast<uint32_t>(128 * g) + (static_cast<uint32_t>(32 * q) << 16);
+      for (uint32_t t = static_cast<uint32_t>(g - static_cast<int>(T0 & 3u) + 4) & 3u; t < ntiles; t += 4) {
         const uint32_t T = T0 + t;
         const uint32_t st = T % kStages, use = T / kStages;
-        if (!mbar_wait(bar(B_HXF + st), use & 1u, s.spin_limit, abort_flag, err, 10)) { ok = false; break; }
-        const uint32_t c0 = t * kTile, cs = c0 + gt;
-        const bool live = cs < s.n_s;
+        if (!warp_wait(bar(B_HXF + st), use & 1u, s.spin_limit, abort_flag, err, 10)) { ok = false; break; }
+        const uint32_t c0 = t * kTile, c = c0 + gt;
+        const bool live = c < s.n_s;
         float v[32];
         uint32_t pos[16];
         uint32_t C = 0xffffu;
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = 0.f;
         if (live) {
-          C = cset[s.cset_off + cs];
+          C = cs_sm[c];
           if (has_own) {
+            // own-row position of C u a (tc::own_pos with its per-set terms hoisted)
+            const uint32_t lomask = (1u << lo) - 1u, P = C & lomask, Q = C >> lo;
+            const int p = __popc(P);
+            const uint32_t top = s.n_own - 1u;
+            const uint32_t base_lo = top - Gt[Q * tc::gw(lo) + p + 1];
+            const uint32_t base_hi = top - c8[P];
 #pragma unroll
             for (int a = 0; a < 16; ++a) {
               if (a < sp && !((C >> a) & 1u)) {
-                pos[a] = tc::own_pos(C, a, s.n_own, lo, c8, Gt);
+                pos[a] = a < lo ? base_lo - c8[P | (1u << a)]
+                                : base_hi - Gt[(Q | (1u << (a - lo))) * tc::gw(lo) + p];
                 v[a] = x_own[pos[a]];
               }
             }
           }
-          const float *sg = stage + st * (16 * kSlot);
+          // hole rows: the staged segment of row h starts at its 16-byte
+          // chunk, (rs + c0) & 3 elements before this tile's first set
+          const float *sg = stage + st * (16 * kSlot) + gt;
 #pragma unroll
           for (int h = 0; h < 16; ++h) {
             if (h < nhr) {
-              const uint32_t gidx = hole_rs[h] + cs;
-              uint32_t a0, a1;
-              tc::hole_segment(hole_rs[h], c0, min(c0 + kTile, s.n_s), s.D, &a0, &a1);
-              v[16 + h] = gidx < a1 ? sg[h * kSlot + (gidx - a0)] : x[gidx];
+              const uint32_t rs = hole_rs[h], gidx = rs + c;
+              v[16 + h] = gidx < Dl ? sg[h * kSlot + ((rs + c0) & 3u)] : x[gidx];
             }
           }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(bar(B_HXE + st));
-        // split and store the row of set gt (8 + 8 16-byte chunks)
-        uint8_t *Ahi = sm + kOffA + g * 32768, *Alo = Ahi + 16384;
+        // split into TF32 high and low parts, both into this set's lane
+        {
+          uint32_t hv[32];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          uint32_t hv[4];
-          float lv[4];
+          for (int j = 0; j < 32; ++j) hv[j] = tf32_rna(v[j]);
+          tc_st32(t_grp, hv);
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            hv[e] = tf32_rna(v[4 * q + e]);
-            lv[e] = v[4 * q + e] - __uint_as_float(hv[e]);
-          }
-          const uint32_t off = sw128(gt, 4 * q);
-          *reinterpret_cast<uint4 *>(Ahi + off) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-          *reinterpret_cast<float4 *>(Alo + off) = make_float4(lv[0], lv[1], lv[2], lv[3]);
+          for (int j = 0; j < 32; ++j) hv[j] = __float_as_uint(v[j] - __uint_as_float(hv[j]));
+          tc_st32(t_grp + 32, hv);
         }
-        fence_async_smem();
+        tc_wait_st();
+        tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(bar(B_AF + g));
-        if (!mbar_wait(bar(B_ACC + g), (T >> 1) & 1u, s.spin_limit, abort_flag, err, 11)) { ok = false; break; }
+        if (!warp_wait(bar(B_ACC + g), (T >> 2) & 1u, s.spin_limit, abort_flag, err, 11)) { ok = false; break; }
         tc_fence_after();
         float yv[32];
-        tc_ld32(tmem + static_cast<uint32_t>(g * 32) + (static_cast<uint32_t>((warp & 3) * 32) << 16), yv);
+        tc_ld32(t_grp + 64, yv);
         tc_fence_before();
         if (live) {
           if (has_own) {
@@ -361,14 +405,14 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
           }
 #pragma unroll
           for (int h = 0; h < 16; ++h)
-            if (h < nhr) atomicAdd(y + hole_rs[h] + cs, yv[16 + h]);
+            if (h < nhr) atomicAdd(y + hole_rs[h] + c, yv[16 + h]);
         }
       }
-    } else if (warp == 8 && ok) {
+    } else if (warp == kProdWarp && ok) {
       // ---- producer: the hole-row segments of every tile of this unit
       for (uint32_t t = 0; t < ntiles; ++t) {
         const uint32_t T = T0 + t, st = T % kStages, use = T / kStages;
-        if (use > 0 && !mbar_wait(bar(B_HXE + st), (use - 1) & 1u, s.spin_limit, abort_flag, err, 12)) {
+        if (use > 0 && !warp_wait(bar(B_HXE + st), (use - 1) & 1u, s.spin_limit, abort_flag, err, 12)) {
           ok = false;
           break;
         }
@@ -385,17 +429,17 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
           bulk_load(su32(stage + st * (16 * kSlot) + lane * kSlot), x + a0, bytes, bar(B_HXF + st));
         loads_issued = T + 1;
       }
-    } else if (warp == 9 && ok) {
+    } else if (warp == kMmaWarp && ok) {
       // ---- MMA issue (one thread): 3 passes x the k-steps that hold columns
       for (uint32_t t = 0; t < ntiles; ++t) {
-        const uint32_t T = T0 + t, g = T & 1u;
-        if (!mbar_wait(bar(B_AF + g), (T >> 1) & 1u, s.spin_limit, abort_flag, err, 13)) {
+        const uint32_t T = T0 + t, g = T & 3u;
+        if (!warp_wait(bar(B_AF + g), (T >> 2) & 1u, s.spin_limit, abort_flag, err, 13)) {
           ok = false;
           break;
         }
         tc_fence_after();
         if (lane == 0) {
-          const uint32_t a_hi = base + kOffA + g * 32768, a_lo = a_hi + 16384;
+          const uint32_t a_hi = tmem + 128u * g, a_lo = a_hi + 32u, d = a_hi + 64u;
           const uint32_t b_hi = base + kOffB, b_lo = b_hi + 4096;
           uint32_t acc = 0;
 #pragma unroll
@@ -405,7 +449,7 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
             for (int ks = 0; ks < 4; ++ks) {
               const bool used = ks == 0 ? true : ks == 1 ? sp > 8 : ks == 2 ? nhr > 0 : nhr > 8;
               if (used) {
-                tc_mma(tmem + g * 32, smem_desc(a + ks * 32), smem_desc(b + ks * 32), acc);
+                tc_mma_ts(d, a + 8u * ks, smem_desc(b + ks * 32), acc);
                 acc = 1;
               }
             }
@@ -431,9 +475,9 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
 
   // ---- drain: after an abort, wait (bounded, with the fixed limit: these are
   // copies and MMAs that complete by themselves) for what is in flight, then
-  // free TMEM
+  // free the tensor memory
   __syncthreads();
-  if (*abort_flag && warp == 8 && lane == 0) {
+  if (*abort_flag && warp == kProdWarp && lane == 0) {
     // the latest request of each stage is complete once that use's phase has completed
     for (uint32_t st = 0; st < kStages; ++st) {
       if (loads_issued > st) {
@@ -444,7 +488,7 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
       }
     }
   }
-  if (warp == 9) {
+  if (warp == kMmaWarp) {
     if (lane == 0 && mma_issued > 0) {
       tc_commit(bar(B_DRAIN));
       for (long i = 0; i < kTcSpinLimit && !mbar_try(bar(B_DRAIN), 0); ++i) {
@@ -455,7 +499,8 @@ sigma_tc_kernel(TcShape s, const uint32_t *__restrict__ g_binom, const uint32_t 
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 9) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+  if (warp == kMmaWarp)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
 // ---------------------------------------------------------------- host side
@@ -524,7 +569,7 @@ bool tc_fits(const doci_ham *h) {
   if (major != 10 || minor != 3) return false;  // built for sm_103a only
   int optin = 0;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  return tc_smem_bytes(static_cast<uint32_t>(h->max_row)) <= static_cast<size_t>(optin);
+  return std::max(tc_smem_bytes(static_cast<uint32_t>(h->max_row)), kMinSmem) <= static_cast<size_t>(optin);
 }
 
 // launches of one sigma: the no-column rows (if any) and one per row-part
@@ -584,7 +629,7 @@ int launch_tc(const doci_ham *h, const float *x, float *y, cudaStream_t st, int 
     s.nhr = na - kp;
     s.spin_limit = spin_limit;
     if (s.n_units == 0 || s.n_s == 0) continue;
-    const size_t smem = tc_smem_bytes(s.n_own);
+    const size_t smem = std::max(tc_smem_bytes(s.n_own), kMinSmem);
     const int grid = static_cast<int>(std::min<uint32_t>(s.n_units, static_cast<uint32_t>(sms)));
     sigma_tc_kernel<<<grid, kTcThreads, smem, st>>>(s, h->d_binom, h->d_rowstart, tb->cset, tb->tables,
                                                     reinterpret_cast<const float *>(h->d_kfrag), h->d_diag32, x, y,

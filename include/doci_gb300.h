@@ -180,9 +180,12 @@ int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int
  * adds), 8 the (N-1)-pair form on the 5th-generation tensor cores (FP32
  * only: the own row of a set's row part staged in shared memory, the other
  * rows streamed by TMA, the product in TMEM, each own row written once;
- * needs a 16-byte aligned x, else kind 6 runs).  Kinds 6 and 8 reduce into
+ * needs a 16-byte aligned x, else kind 6 runs), 9 the phase-ordered row
+ * pass in float-float arithmetic (FP64 only: FP64 accuracy from pairs of
+ * FP32 values, x converted once per call into stream-ordered scratch of D x 8
+ * bytes; FP32 requests for it use the automatic choice).  Kinds 6 and 8 reduce into
  * sigma with atomic adds, so their last bits vary between runs; FP64
- * requests for them use the automatic choice.  3-8 fall back to 1 when the
+ * requests for them use the automatic choice.  3-9 fall back to 1 when the
  * handle has no row tiling.  Other values: DOCI_ERR_INVALID.  A device wait
  * of kind 8 that runs out (it never should) is reported as
  * DOCI_ERR_DEVICE_TIMEOUT by the handle's next synchronous call
@@ -203,7 +206,7 @@ int doci_ham_set_sigma_kernel(doci_ham *ham, int kind);
 int doci_ham_autotune(doci_ham *ham, int precision, int nvec, int *choice);
 
 /* The path doci_sigma takes for this handle and precision: *kind as in
- * doci_ham_set_sigma_kernel (1, 3, 4, 6 or 8; the automatic choice resolved) and
+ * doci_ham_set_sigma_kernel (1, 3, 4, 6, 8 or 9; the automatic choice resolved) and
  * *launches, the number of kernel launches of one call.  Host-only query. */
 int doci_sigma_plan(const doci_ham *ham, int precision, int *kind, int *launches);
 
@@ -242,7 +245,10 @@ int doci_multidot(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n
  * array's device address (cudaGetSymbolAddress), so make it before any
  * stream capture.  All calls share the array: calls that overlap on the GPU
  * (other streams, other host threads) race and must be serialised by the
- * caller.  Allocates nothing, frees nothing. */
+ * caller.  The looked-up address is kept for the life of the process: after
+ * cudaDeviceReset on a device (which unloads the library's device image
+ * there, as it invalidates every handle) do not call it on that device
+ * again.  Allocates nothing, frees nothing. */
 int doci_multidot_noalloc(const void *d_V, int64_t ld, int m, const void *d_w, int64_t n, int precision,
                           double *d_out, void *stream);
 

@@ -118,6 +118,12 @@ int main(int argc, char **argv) {
             const uint32_t g = hole_rs[h] + cs;
             if (g < a0) fail("segment start", g, a0);
             if (g < a1 && g - a0 >= kSlot) fail("slot index", g - a0, kSlot);
+            // the kernel reads the staged copy below the vector's last whole
+            // 16-byte chunk, at slot index ((rs + c0) & 3) + (cs - c0)
+            if (g < (static_cast<uint32_t>(D) & ~3u)) {
+              if (g >= a1) fail("staged element not copied", g, a1);
+              if (((hole_rs[h] + c0) & 3u) + (cs - c0) != g - a0) fail("kernel slot index", g, a0);
+            }
             if (g >= D) fail("hole index", g, (long)D);
           }
         }

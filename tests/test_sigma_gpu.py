@@ -50,7 +50,7 @@ def test_golden_sigma_diag_bits(name, fcidump, dg):
         assert np.array_equal(ranks.cpu().numpy(), np.arange(h.D))
 
 
-@pytest.mark.parametrize("kernel", ["auto", "gather", "row1", "rowx", "pair", "tc"])
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row1", "rowx", "pair", "tc", "rowff"])
 @pytest.mark.parametrize("L,N,seed", [(16, 8, 21), (18, 5, 22), (20, 10, 23), (12, 1, 24), (12, 11, 25),
                                       (7, 0, 26), (6, 6, 27), (32, 2, 28), (32, 30, 29), (24, 12, 30),
                                       (22, 11, 31), (26, 4, 32)])
@@ -91,7 +91,7 @@ def test_addressing_full_size_properties(synth, dg):
             assert all(bin(int(v)).count("1") == 16 for v in b[:64])
 
 
-@pytest.mark.parametrize("kernel", ["auto", "gather", "row1", "rowx", "pair", "tc"])
+@pytest.mark.parametrize("kernel", ["auto", "gather", "row1", "rowx", "pair", "tc", "rowff"])
 def test_sigma_full_size_symmetry_and_linearity(kernel, synth, dg):
     """L=28, N=14 (D = 40,116,600): H is symmetric, sigma is linear, and
     sampled rows agree with the oracle's gather form."""
@@ -153,7 +153,7 @@ def test_sigma_L32_fp32_vs_oracle_samples(kernel, synth, dg):
         assert bad.size == 0, (kernel, int(rows[bad[0]]), float(got[bad[0]]), float(ref[bad[0]]), int(bad.size))
 
 
-@pytest.mark.parametrize("kernel", ["auto", "rowx", "gather"])
+@pytest.mark.parametrize("kernel", ["auto", "rowx", "gather", "rowff"])
 def test_sigma_L32_fp64_vs_oracle_samples(kernel, synth, dg):
     """L=32, N=16 (D = 601,080,390), FP64 (the anchor and verification sigma
     of every mixed solve at this size): sampled rank windows across the whole
@@ -261,7 +261,10 @@ def test_sigma_plan(synth, dg):
         h.set_sigma_kernel("tc")
         assert h.sigma_plan(dg.FP32) == (8, 11)
         assert h.sigma_plan(dg.FP64) == auto64
-        for bad in (2, 5, 7, 9, -1):
+        h.set_sigma_kernel("rowff")
+        assert h.sigma_plan(dg.FP64) == (9, 2)
+        assert h.sigma_plan(dg.FP32) == (6, 2)  # FP64 only
+        for bad in (2, 5, 7, 10, -1):
             with pytest.raises(dg.DociError):
                 h.set_sigma_kernel(bad)
     with dg.Hamiltonian.from_fcidump(synth(12, 6, 52)) as h:
