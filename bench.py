@@ -306,8 +306,9 @@ def pct(v, q):
 
 def batch_workload(a):
     """Many seeded Hamiltonians (L uniform in [lmin, lmax], N = L // 2), the
-    `roots` lowest eigenpairs each, mixed precision; batched (workers solves
-    in flight) against one at a time (a sample)."""
+    `roots` lowest eigenpairs each, mixed precision; the whole batch in the
+    batch engine (lockstep, graph-captured iterations) against one at a time
+    through the same engine (a sample spread over the batch)."""
     import numpy as np
     import doci_gb300 as dg
     from doci_gb300.fcidump import raw_integrals
@@ -320,14 +321,13 @@ def batch_workload(a):
         one, two = raw_integrals(int(L), 1000 + i)
         hams.append(dg.Hamiltonian.from_integrals(int(L), int(L) // 2, 0.0, one, two))
     t_build = time.perf_counter() - t0
-    # autotune the sigma paths once per (L, N) shape (process-wide choices),
-    # before both the sequential and the batched runs
+    # the batch engine's sigma tile shape, tuned once per (L, N) shape
+    # (process-wide choices), before both the sequential and the batched runs
     t0 = time.perf_counter()
     tuned = {}
     for i, L in enumerate(Ls):
         if int(L) not in tuned:
-            nv = min(4, a.roots)
-            tuned[int(L)] = [hams[i].autotune(p, n) for p in (dg.FP32, dg.FP64) for n in sorted({1, nv})]
+            tuned[int(L)] = hams[i].engine_autotune(min(8, a.roots))
     t_tune = time.perf_counter() - t0
     opts = dict(nroots=a.roots, tol=1e-5, mode="mixed", mixed_tol=1e-3, max_vec=min(32, max(16, 8 * a.roots)))
     k = min(a.sequential_sample, a.problems)
@@ -336,7 +336,7 @@ def batch_workload(a):
     seq = [dg.solve_roots(hams[i], **opts) for i in idx]
     t_seq = time.perf_counter() - t0
     t0 = time.perf_counter()
-    st, res = dg.batch_solve(hams, workers=a.workers, **opts)
+    st, res = dg.batch_solve(hams, **opts)
     t_bat = time.perf_counter() - t0
     same = all(res[i]["energies"] == seq[j]["energies"] for j, i in enumerate(idx))
     lat = [r["end_s"] - r["queued_s"] for r in res]
@@ -348,9 +348,9 @@ def batch_workload(a):
             "speedup_vs_one_at_a_time": round((a.problems / t_bat) / (k / t_seq), 3),
             "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99), "same_alone_and_in_batch": same,
             "converged": int(sum(r["converged"] for r in res)), "build_s": round(t_build, 2),
-            "autotune_s": round(t_tune, 2), "tuned": {str(k): v for k, v in sorted(tuned.items())},
+            "autotune_s": round(t_tune, 2), "tile_dets_per_thread": {str(k): v for k, v in sorted(tuned.items())},
             "config": {"workload": f"{a.problems} Hamiltonians, L uniform in {lmin}..{lmax}, N=L//2, "
-                                   f"{a.roots} roots, workers={a.workers}", "opts": opts,
+                                   f"{a.roots} roots", "opts": opts,
                        "sequential_sample": k}}
     print(json.dumps(line), flush=True)
 

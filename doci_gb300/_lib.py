@@ -108,6 +108,7 @@ def lib() -> C.CDLL:
         "doci_sigma_plan": (i, [vp, i, C.POINTER(i), C.POINTER(i)]),
         "doci_ham_autotune": (i, [vp, i, i, C.POINTER(i)]),
         "doci_sigma_host": (i, [vp, vp, vp, i]),
+        "doci_engine_autotune": (i, [vp, i, vp]),
         "doci_ham_set_sigma_kernel": (i, [vp, i]),
         "doci_bitstrings": (i, [vp, i64, i64, vp, vp]),
         "doci_ranks": (i, [vp, vp, i64, vp, vp]),
@@ -219,6 +220,13 @@ class Hamiltonian:
 
     def __exit__(self, *a):
         self.close()
+
+    def engine_autotune(self, nvec: int = 1) -> int:
+        """The batch engine's sigma tile (determinants per thread) for this
+        shape, timed and kept for the process; doci_engine_autotune."""
+        d = C.c_int()
+        _check(lib().doci_engine_autotune(self._h, int(nvec), C.byref(d)), "doci_engine_autotune")
+        return d.value
 
     def set_sigma_kernel(self, kind) -> None:
         """0/'auto', 1/'gather', 3/'row1' (row pass), 4/'rowx' (phase-ordered row pass),

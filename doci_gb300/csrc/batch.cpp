@@ -2,12 +2,15 @@
 // request server (continuous batching with HBM-footprint admission).
 //
 // No counterpart in the reference (single Hamiltonian, single root,
-// davidson.c:90 / :117 use the lowest eigenvalue only).  Every solve runs the
-// device-resident block Davidson (solvers.cu) on its own CUDA stream; a pool
-// of host workers keeps several solves in flight so that their kernels
-// overlap on the GPU.  A solve's arithmetic does not depend on what else runs
-// (fixed grids, fixed-order reductions, no atomics), so a result is the same
-// alone and in the mix.
+// davidson.c:90 / :117 use the lowest eigenvalue only).  Every solve runs on
+// the batch engine (engine.cu): doci_batch_solve hands it the whole batch
+// (in groups that fit the HBM budget), one lockstep iteration for all
+// problems; doci_solve_roots and the request server's workers hand it one
+// problem each, and the server keeps several such solves in flight on their
+// own streams so that their kernels overlap on the GPU.  A problem's
+// arithmetic in the engine does not depend on the other problems (fixed
+// chunks, fixed-order reductions, no atomics), so a result is the same alone,
+// in a batch and in the server's mix.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -22,143 +25,26 @@
 #include <thread>
 #include <vector>
 
+#include "engine.h"
 #include "internal.h"
-#include "solvers.h"
-#include "vec.h"
-
-namespace doci {
-int vec_argmin(const double *d, size_t n, int64_t *idx, cudaStream_t st);
-int vec_set_unit(double *t, size_t n, int64_t idx, cudaStream_t st);
-}  // namespace doci
 
 using namespace doci;
 
 namespace {
 
-struct StreamBuf {
-  void *p = nullptr;
-  cudaStream_t st = nullptr;
-  StreamBuf() = default;
-  StreamBuf(const StreamBuf &) = delete;
-  StreamBuf &operator=(const StreamBuf &) = delete;
-  ~StreamBuf() {
-    if (p) cudaFreeAsync(p, st);
-  }
-  int alloc(size_t bytes, cudaStream_t s) {
-    st = s;
-    DOCI_CUDA(cudaMallocAsync(&p, bytes ? bytes : 16, s));
-    return DOCI_OK;
-  }
-};
-
-#define DOCI_TRY_B(expr)            \
-  do {                              \
-    const int _st = (expr);         \
-    if (_st != DOCI_OK) return _st; \
-  } while (0)
-
-// nroots start vectors: unit vectors on the nroots lowest diagonal elements
-// (the HF start of executable.c:276-288, extended to several roots)
-int start_vectors(doci_ham *h, int R, double *d_T, cudaStream_t st) {
-  const size_t D = h->D;
-  StreamBuf tmp;
-  DOCI_TRY_B(tmp.alloc(sizeof(double) * D, st));
-  double *d = static_cast<double *>(tmp.p);
-  DOCI_CUDA(cudaMemcpyAsync(d, h->d_diag, sizeof(double) * D, cudaMemcpyDeviceToDevice, st));
-  const double inf = 1e308;
-  for (int r = 0; r < R; ++r) {
-    int64_t idx = 0;
-    DOCI_TRY_B(vec_argmin(d, D, &idx, st));
-    DOCI_TRY_B(vec_set_unit(d_T + static_cast<size_t>(r) * D, D, idx, st));
-    DOCI_CUDA(cudaMemcpyAsync(d + idx, &inf, sizeof(double), cudaMemcpyHostToDevice, st));
-    DOCI_CUDA(cudaStreamSynchronize(st));
-  }
-  return DOCI_OK;
-}
-
 double clock_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// The solve of one Hamiltonian for the nroots lowest eigenpairs, on stream st.
+// The solve of one Hamiltonian for the nroots lowest eigenpairs, on stream st:
+// the batch engine with a batch of one (the same arithmetic as in any batch).
 int solve_roots(doci_ham *h, const doci_batch_opts &o, cudaStream_t st, doci_root_result *res, double *vecs) {
-  const int R = o.nroots;
-  if (R < 1 || R > 8 || static_cast<uint64_t>(R) > h->D) return DOCI_ERR_INVALID;
-  const size_t D = h->D;
-  MatvecOp op;
-  op.ham = h;
-  op.n = D;
-  StreamBuf X, T;
-  DOCI_TRY_B(X.alloc(sizeof(double) * D * R, st));
-  DOCI_TRY_B(T.alloc(sizeof(double) * D * R, st));
-  double *d_X = static_cast<double *>(X.p), *d_T = static_cast<double *>(T.p);
-  DOCI_TRY_B(start_vectors(h, R, d_T, st));
-  BlockArgs a;
-  a.nroots = R;
-  a.max_vectors = o.max_vec < 2 * R ? 2 * R : o.max_vec;
-  if (a.max_vectors > 32) a.max_vectors = 32;
-  // thick restart: by default keep 2 nroots Ritz vectors, at least a quarter
-  // of the basis (keeping only the nroots wanted ones restarts every few
-  // blocks and stalls the higher roots: measured on 40 of the batch
-  // workload's problems, 4 roots, 30/40 converged within 200 iterations with
-  // keep = 4 against 40/40 with keep = 8)
-  a.keep = o.keep > 0 ? o.keep : std::max(2 * R, a.max_vectors / 4);
-  if (a.keep < R) a.keep = R;
-  if (a.keep > a.max_vectors - R) a.keep = a.max_vectors - R;
-  a.max_its = o.max_its;
-  a.tol = o.tol;
-  BlockOut out;
-  int its32 = 0;
-  if (o.mode == DOCI_MODE_MIXED) {
-    StreamBuf T32;
-    DOCI_TRY_B(T32.alloc(sizeof(float) * D * R, st));
-    DOCI_TRY_B((vec_convert<double, float>(d_T, static_cast<float *>(T32.p), D * R, st)));
-    BlockArgs a32 = a;
-    a32.tol = o.mixed_tol > o.tol ? o.mixed_tol : o.tol;
-    a32.stall_window = 15;
-    // the FP32 phase runs on H - (lowest diagonal element)
-    ShiftedView sv;
-    DOCI_TRY_B(sv.make(h, st));
-    a32.shift = sv.shift;
-    MatvecOp op32;
-    op32.ham = &sv.view;
-    op32.n = D;
-    BlockOut o32;
-    DOCI_TRY_B(block_davidson_run<float>(op32, D, h->d_diag, static_cast<float *>(T32.p), a32, st, &o32, d_X));
-    its32 = o32.iterations;
-    for (int r = 0; r < R; ++r) res->energy_fp32[r] = o32.energy[r];
-    DOCI_CUDA(cudaMemcpyAsync(d_T, d_X, sizeof(double) * D * R, cudaMemcpyDeviceToDevice, st));
-    a.max_its = o.max_its - its32 > 1 ? o.max_its - its32 : 1;
-    out.sigmas = o32.sigmas;
-  }
-  DOCI_TRY_B(block_davidson_run<double>(op, D, h->d_diag, d_T, a, st, &out, d_X));
-  res->nroots = R;
-  for (int r = 0; r < R; ++r) {
-    res->energy[r] = out.energy[r];
-    res->residual[r] = out.residual[r];
-  }
-  res->iterations = out.iterations + its32;
-  res->iterations_fp32 = its32;
-  res->sigmas = out.sigmas;
-  res->converged = out.converged;
-  if (vecs) {
-    DOCI_CUDA(cudaMemcpyAsync(vecs, d_X, sizeof(double) * D * R, cudaMemcpyDeviceToHost, st));
-  }
-  DOCI_CUDA(cudaStreamSynchronize(st));
-  return DOCI_OK;
+  if (o.nroots < 1 || o.nroots > 8 || static_cast<uint64_t>(o.nroots) > h->D) return DOCI_ERR_INVALID;
+  double *const v[1] = {vecs};
+  return engine_solve(1, &h, o, st, res, v);
 }
 
-int64_t roots_footprint(int L, int N, const doci_batch_opts &o) {
-  if (L < 1 || L > 32 || N < 0 || N > L) return -1;
-  const int64_t D = static_cast<int64_t>(binom64(L, N));
-  const int64_t R = o.nroots, mv = std::min(32, std::max(o.max_vec, 2 * o.nroots));
-  const int64_t ham = D * 12 + (16ll << 20);  // diagonals, tables
-  const int64_t common = D * R * 8 * 2 + D * 8;  // X, T, start-vector scratch
-  const int64_t p64 = 2 * mv * D * 8 + R * D * 8;
-  // FP32 phase: basis, start and correction blocks, shifted FP32 diagonal
-  const int64_t p32 = o.mode == DOCI_MODE_MIXED ? 2 * mv * D * 4 + R * D * 4 * 2 + D * 4 : 0;
-  return ham + common + std::max(p64, p32) + (4ll << 20);
-}
+int64_t roots_footprint(int L, int N, const doci_batch_opts &o) { return engine_footprint(L, N, o); }
 
 }  // namespace
 
@@ -310,6 +196,11 @@ int64_t doci_roots_footprint(int L, int n_pairs, const doci_batch_opts *o) {
   return roots_footprint(L, n_pairs, *o);
 }
 
+int doci_engine_autotune(doci_ham *h, int nvec, int *dets_per_thread) {
+  if (!h) return DOCI_ERR_INVALID;
+  return engine_tune(h, nvec, dets_per_thread);
+}
+
 int doci_solve_roots(doci_ham *h, const doci_batch_opts *opts, doci_root_result *res, double *vecs) {
   if (!h || !res) return DOCI_ERR_INVALID;
   doci_batch_opts o;
@@ -413,21 +304,50 @@ void doci_server_destroy(doci_server *srv) {
 
 int doci_batch_solve(int n, doci_ham *const *hams, const doci_batch_opts *opts, doci_root_result *results) {
   if (n < 0 || (n > 0 && (!hams || !results))) return DOCI_ERR_INVALID;
-  doci_server *srv = nullptr;
-  int s = doci_server_create(opts, &srv);
-  if (s) return s;
-  std::vector<int64_t> tickets(n);
+  if (n == 0) return DOCI_OK;
+  doci_batch_opts o;
+  if (opts) o = *opts; else doci_batch_opts_default(&o);
   for (int i = 0; i < n; ++i) {
-    doci_server::Req r;
-    r.ham = hams[i];
-    tickets[i] = srv->submit(std::move(r));
+    if (!hams[i]) return DOCI_ERR_INVALID;
+    std::memset(&results[i], 0, sizeof results[i]);
   }
+  int64_t budget = o.hbm_budget;
+  if (budget <= 0) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+      cudaGetLastError();
+      return DOCI_ERR_NO_DEVICE;
+    }
+    budget = static_cast<int64_t>(fr * 0.85);
+  }
+  cudaStream_t st = nullptr;
+  DOCI_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  const double t0 = clock_s();
   int first_err = DOCI_OK;
-  for (int i = 0; i < n; ++i) {
-    doci_server_wait(srv, tickets[i], &results[i]);
-    if (results[i].status != DOCI_OK && first_err == DOCI_OK) first_err = results[i].status;
+  // groups of consecutive problems whose engine footprint fits the budget
+  // (the handles' own memory is already allocated: count the solve's share)
+  for (int i = 0; i < n;) {
+    int64_t used = 0;
+    int j = i;
+    while (j < n) {
+      const int64_t f = engine_footprint(hams[j]->L, hams[j]->N, o) - static_cast<int64_t>(hams[j]->D) * 12;
+      if (j > i && used + f > budget) break;
+      used += f;
+      ++j;
+    }
+    const double ts = clock_s() - t0;
+    int s = (used > budget) ? DOCI_ERR_ADMISSION : engine_solve(j - i, hams + i, o, st, results + i, nullptr);
+    const double te = clock_s() - t0;
+    for (int k = i; k < j; ++k) {
+      results[k].status = s;
+      results[k].queued_s = 0;
+      results[k].start_s = ts;
+      results[k].end_s = te;
+    }
+    if (s != DOCI_OK && first_err == DOCI_OK) first_err = s;
+    i = j;
   }
-  doci_server_destroy(srv);
+  cudaStreamDestroy(st);
   return first_err;
 }
 

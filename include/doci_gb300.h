@@ -323,7 +323,7 @@ typedef struct doci_batch_opts {
   double tol;          /* residual-norm tolerance of every root (1e-6) */
   int mode;            /* DOCI_MODE_MIXED (default) or DOCI_MODE_FP64 */
   double mixed_tol;    /* residual at which the FP32 phase hands over (1e-4) */
-  int workers;         /* solves in flight at once, one CUDA stream each (8) */
+  int workers;         /* server: solves in flight at once, one CUDA stream each (8) */
   int64_t hbm_budget;  /* device bytes the solves in flight may hold; 0 = 85% of free */
   int keep;            /* basis vectors kept at a thick restart, nroots..max_vec - nroots;
                           0 = automatic (max(2 nroots, max_vec / 4)) */
@@ -344,12 +344,28 @@ void doci_batch_opts_default(doci_batch_opts *opts);
 int64_t doci_roots_footprint(int L, int n_pairs, const doci_batch_opts *opts);
 
 /* Block-Davidson solve for the opts->nroots lowest eigenpairs (start vectors:
- * unit vectors on the lowest diagonal elements); vecs (host, D x nroots,
- * column-major) may be NULL. */
+ * unit vectors on the lowest diagonal elements) on the batch engine with a
+ * batch of one, so that the result is bit-identical to the same problem's in
+ * doci_batch_solve or the server; vecs (host, D x nroots, column-major) may
+ * be NULL. */
 int doci_solve_roots(doci_ham *ham, const doci_batch_opts *opts, doci_root_result *result, double *vecs);
 
-/* Solve many Hamiltonians: up to opts->workers solves in flight on their own
- * streams, admitted against opts->hbm_budget.  results[i] for hams[i]. */
+/* Tile autotuning of the batch engine: time its sigma's tile shapes (1, 2 or
+ * 4 determinants per thread of a 256-thread tile) on this handle with nvec
+ * (1..8) vectors and keep the fastest for every problem of the same
+ * (device, L, n_pairs) in the process; *dets_per_thread receives it (may be
+ * NULL).  Changes no result (each determinant's sum is the same in every
+ * tile shape).  Synchronous.  No counterpart in the reference. */
+int doci_engine_autotune(doci_ham *ham, int nvec, int *dets_per_thread);
+
+/* Solve many Hamiltonians at once on the batch engine: every problem of a
+ * group advances in lockstep, one device-resident, graph-captured block
+ * Davidson iteration for the whole group (batched sigma over a shared space
+ * of determinant tiles, batched vector passes, one subspace eigensolver per
+ * problem on the device); groups are formed in order so that their solves
+ * fit opts->hbm_budget (0: 85% of the free memory).  A result does not
+ * depend on the rest of the batch.  results[i] for hams[i] (start_s / end_s:
+ * the group's run, seconds from the call). */
 int doci_batch_solve(int n, doci_ham *const *hams, const doci_batch_opts *opts, doci_root_result *results);
 
 /* Request server: submitted requests (integrals or an FCIDUMP path) are
