@@ -25,6 +25,7 @@ import doci_gb300 as dg, oracle
 p = {path!r}
 o = oracle.Ham(p)
 with dg.Hamiltonian.from_fcidump(p) as h:
+    h.set_sigma_kernel("tc")
     assert h.sigma_plan(dg.FP32)[0] == 8, h.sigma_plan(dg.FP32)
     x = np.random.default_rng(1).standard_normal(h.D).astype(np.float32)
     y = np.empty_like(x)
