@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-7, help="solve: residual tolerance")
     ap.add_argument("--mixed-tol", type=float, default=1e-4,
                     help="residual that ends the FP32 phase of the time-to-converge run")
+    ap.add_argument("--batch-mixed-tol", type=float, default=1e-3,
+                    help="batch / serve: residual that ends the FP32 phase of each solve")
     return ap.parse_args()
 
 
@@ -329,7 +331,8 @@ def batch_workload(a):
         if int(L) not in tuned:
             tuned[int(L)] = hams[i].engine_autotune(min(8, a.roots))
     t_tune = time.perf_counter() - t0
-    opts = dict(nroots=a.roots, tol=1e-5, mode="mixed", mixed_tol=1e-3, max_vec=min(32, max(16, 8 * a.roots)))
+    opts = dict(nroots=a.roots, tol=1e-5, mode="mixed", mixed_tol=a.batch_mixed_tol,
+                max_vec=min(32, max(16, 8 * a.roots)))
     k = min(a.sequential_sample, a.problems)
     idx = np.linspace(0, a.problems - 1, k).astype(int)
     t0 = time.perf_counter()
@@ -375,7 +378,7 @@ def serve_workload(a):
         L = int(rng.integers(lmin, lmax + 1))
         N = max(1, min(L - 1, L // 2 + int(rng.integers(-2, 3))))
         shapes.append((L, N))
-    opts = dict(nroots=1, tol=1e-6, mode="mixed", mixed_tol=1e-3, max_its=400)
+    opts = dict(nroots=1, tol=1e-6, mode="mixed", mixed_tol=a.batch_mixed_tol, max_its=400)
     ints = [raw_integrals(L, 2000 + i) for i, (L, N) in enumerate(shapes)]  # made before the stream starts
     tickets, conc = [], []
     with dg.Server(workers=a.workers, **opts) as srv:

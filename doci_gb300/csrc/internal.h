@@ -141,6 +141,9 @@ int kernel_blocks(const void *kernel, int threads, size_t dyn, int *blocks);
 // pair-form sigma (sigma_pair.cu), FP32 only
 bool pair_fits(const doci_ham *h);
 int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t s);
+// FP64-accurate pair form in float-float arithmetic (sigma_pair.cu)
+bool pair_ff_fits(const doci_ham *h);
+int launch_pair_ff(const doci_ham *h, const double *x, double *y, cudaStream_t s);
 // tensor-core pair form (sigma_tc.cu), FP32 only, sm_103a; x 16-byte aligned.
 // A device wait that runs out writes a nonzero code to *d_err (spin_limit:
 // try_wait iterations per wait).

@@ -845,9 +845,11 @@ SigmaPlan plan_kind(const doci_ham *h, int precision, bool allow_pair, int kind)
     const bool want_pair = kind == 6 || kind == 8 || (kind == 0 && h->npblocks >= device_sm_count());
     if (want_pair && pair_fits(h)) return {6, 2};  // init pass + pair pass
   }
-  // float-float phase-ordered row pass (FP64 accuracy in FP32 arithmetic):
-  // the x conversion and the row pass
-  if (kind == 9 && precision == DOCI_FP64 && h->nrows >= 1 && rowx_fits(h, sizeof(ff))) return {9, 2};
+  // float-float sigma (FP64 accuracy in FP32 arithmetic): the pair form, or
+  // the phase-ordered row pass where the pair tiling does not fit; the x
+  // conversion (with sigma = diag x for the pair form) and the pass
+  if (kind == 9 && precision == DOCI_FP64 && (pair_ff_fits(h) || (h->nrows >= 1 && rowx_fits(h, sizeof(ff)))))
+    return {9, 2};
   // row kernel when the row tiling exists, fits, and gives every SM work
   bool row = kind >= 3 || (kind == 0 && h->nrows >= device_sm_count());
   if (row && !row_kernel_fits(h, elem)) row = false;
@@ -898,6 +900,8 @@ int launch_sigma(const doci_ham *h, const void *x, void *y, int precision, cudaS
     case 4:
       return f64 ? launch_rowx<double>(h, x, y, st, 1) : launch_rowx<float>(h, x, y, st, 1);
     case 9:
+      // the pair form where it fits, else the phase-ordered row pass, both in float-float
+      if (pair_ff_fits(h)) return launch_pair_ff(h, static_cast<const double *>(x), static_cast<double *>(y), st);
       return launch_rowx_ff(h, static_cast<const double *>(x), static_cast<double *>(y), st);
     default:  // 3
       return f64 ? launch_row<double>(h, x, y, st, 1) : launch_row<float>(h, x, y, st, 1);

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "addressing.cuh"
+#include "ff.cuh"
 #include "internal.h"
 
 namespace doci {
@@ -232,6 +233,96 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP64-accurate pair form in float-float arithmetic (kind 9).  Same blocks
+// and neighbour tables as the kernel above; per set (one per thread) the
+// L - N + 1 open slots (the column-part holes of C', from the insertion
+// table, then the row-part holes of R') hold X_S, and every output
+// Y_S[i] = sum_a K_ia X_S[a] over the open slots is formed in float-float
+// (ff.cuh: about 48 significant bits) from x pre-converted to float-float,
+// converted to double once and added to sigma with an FP64 atomic add
+// (sigma starts as diag * x in FP64).  GB300's FP64 units run at a small
+// fraction of its FP32 rate: the products and sums go to the FP32 units.
+template <int NO>
+__global__ void __launch_bounds__(kPairThreads, 2)
+sigma_pair_ff_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t *__restrict__ rowstart_of,
+                     const uint32_t *__restrict__ g_binom, const double *__restrict__ g_K,
+                     const uint32_t *__restrict__ ins, const uint32_t *__restrict__ ins_off, const ff *__restrict__ x,
+                     double *__restrict__ y) {
+  __shared__ ff Kc[32 * 32];  // K on the block's slots: [output slot][input slot]
+  __shared__ uint32_t hole_rs[32];
+  __shared__ int hole_o[32];
+  const uint32_t *B = g_binom;
+  const int sp = s.split, lane = threadIdx.x & 31;
+  for (int blk = blockIdx.x; blk < s.nblocks; blk += gridDim.x) {
+    const uint2 bw = blocks[blk];
+    const uint32_t own = bw.x, mask = bw.y & 0xffffffu;
+    const int kp = static_cast<int>(bw.y >> 24), jp = s.N - 1 - kp;
+    const int nhr = s.na - kp, keff = sp + nhr, nch = sp - jp, nopen = nch + nhr;
+    __syncthreads();  // the previous block is done with the tables
+    if (threadIdx.x < 32) {
+      const bool hole = lane < s.na && !((mask >> lane) & 1u);
+      const uint32_t hb = __ballot_sync(0xffffffffu, hole);
+      if (hole) {
+        const int h = __popc(hb & ((1u << lane) - 1u));
+        hole_rs[h] = rowstart_of[mask | (1u << lane)];
+        hole_o[h] = sp + lane;
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+      const int i = e >> 5, a = e & 31;
+      const int oi = i < sp ? i : i < keff ? hole_o[i - sp] : -1;
+      const int oa = a < sp ? a : a < keff ? hole_o[a - sp] : -1;
+      Kc[e] = (oi >= 0 && oa >= 0) ? ff_from(g_K[oi * 32 + oa]) : ff(0);
+    }
+    __syncthreads();
+    const uint32_t n_s = __ldg(B + sp * kBinomCols + jp);
+    const uint32_t *ins_blk = ins + ins_off[jp];
+    for (uint32_t c = threadIdx.x; c < n_s; c += blockDim.x) {
+      ff X[NO];
+      uint32_t tgt[NO];
+      int slot[NO];
+      const uint32_t *ip = ins_blk + 16u * c;
+#pragma unroll
+      for (int t = 0; t < NO; ++t) {
+        if (t < nch) {
+          const uint32_t e = __ldg(ip + t);
+          slot[t] = static_cast<int>(e & 0xffu);
+          tgt[t] = own + (e >> 8);
+        } else if (t < nopen) {
+          slot[t] = sp + (t - nch);
+          tgt[t] = hole_rs[t - nch] + c;
+        } else {
+          slot[t] = 0;
+          tgt[t] = 0;
+        }
+        X[t] = t < nopen ? ldg_val(x + tgt[t]) : ff(0);
+      }
+#pragma unroll
+      for (int to = 0; to < NO; ++to) {
+        if (to < nopen) {
+          const ff *Krow = Kc + slot[to] * 32;
+          ff acc(0);
+#pragma unroll
+          for (int ti = 0; ti < NO; ++ti)
+            if (ti < nopen) acc += Krow[slot[ti]] * X[ti];
+          atomicAdd(y + tgt[to], ff_to(acc));
+        }
+      }
+    }
+  }
+}
+
+__global__ void pair_init64_kernel(uint32_t D, const double *__restrict__ diag, const double *__restrict__ x,
+                                   double *__restrict__ y, ff *__restrict__ xf) {
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < D; t += gridDim.x * blockDim.x) {
+    const double v = x[t];
+    y[t] = diag[t] * v;
+    xf[t] = ff_from(v);
+  }
+}
+
 float round_tf32(double v) {
   // nearest TF32 (10-bit mantissa), ties away from zero, as cvt.rna
   float f = static_cast<float>(v);
@@ -311,6 +402,51 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
                                                    h->d_tab_off, x, y);
   DOCI_CUDA(cudaGetLastError());
   return DOCI_OK;
+}
+
+bool pair_ff_fits(const doci_ham *h) { return pair_fits(h) && h->L - h->N + 1 <= 32; }
+
+// open slots per set: L - N + 1
+template <int NO>
+int launch_pair_ff_no(const doci_ham *h, const double *x, double *y, cudaStream_t st) {
+  const int sms = device_sm_count();
+  ff *xf = nullptr;
+  DOCI_CUDA(cudaMallocAsync(&xf, sizeof(ff) * static_cast<size_t>(h->D), st));
+  {
+    uint64_t grid = (static_cast<uint64_t>(h->D) + 255) / 256;
+    const uint64_t cap = static_cast<uint64_t>(sms) * 8;
+    if (grid > cap) grid = cap;
+    pair_init64_kernel<<<static_cast<unsigned>(grid), 256, 0, st>>>(h->D, h->d_diag, x, y, xf);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, h->npblocks};
+    int per_sm = 1;
+    const int r = kernel_blocks(reinterpret_cast<const void *>(sigma_pair_ff_kernel<NO>), kPairThreads, 0, &per_sm);
+    if (r != DOCI_OK) {
+      cudaFreeAsync(xf, st);
+      return r;
+    }
+    int grid = sms * per_sm;
+    if (grid > h->npblocks) grid = h->npblocks;
+    sigma_pair_ff_kernel<NO><<<grid, kPairThreads, 0, st>>>(s, reinterpret_cast<const uint2 *>(h->d_pblocks),
+                                                            h->d_rowstart, h->d_binom, h->d_Kmir64, h->d_ins,
+                                                            h->d_tab_off, xf, y);
+    e = cudaGetLastError();
+  }
+  const cudaError_t ef = cudaFreeAsync(xf, st);
+  DOCI_CUDA(e);
+  DOCI_CUDA(ef);
+  return DOCI_OK;
+}
+
+int launch_pair_ff(const doci_ham *h, const double *x, double *y, cudaStream_t st) {
+  if (!pair_ff_fits(h)) return DOCI_ERR_INVALID;
+  const int no = h->L - h->N + 1;
+  if (no <= 8) return launch_pair_ff_no<8>(h, x, y, st);
+  if (no <= 17) return launch_pair_ff_no<17>(h, x, y, st);
+  if (no <= 24) return launch_pair_ff_no<24>(h, x, y, st);
+  return launch_pair_ff_no<32>(h, x, y, st);
 }
 
 }  // namespace doci
