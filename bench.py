@@ -79,7 +79,7 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-7, help="solve: residual tolerance")
     ap.add_argument("--mixed-tol", type=float, default=1e-4,
                     help="residual that ends the FP32 phase of the time-to-converge run")
-    ap.add_argument("--batch-mixed-tol", type=float, default=1e-3,
+    ap.add_argument("--batch-mixed-tol", type=float, default=1e-5,
                     help="batch / serve: residual that ends the FP32 phase of each solve")
     return ap.parse_args()
 
@@ -342,6 +342,7 @@ def batch_workload(a):
     st, res = dg.batch_solve(hams, **opts)
     t_bat = time.perf_counter() - t0
     same = all(res[i]["energies"] == seq[j]["energies"] for j, i in enumerate(idx))
+    dE_alone = max(max(abs(u - v) for u, v in zip(res[i]["energies"], seq[j]["energies"])) for j, i in enumerate(idx))
     lat = [r["end_s"] - r["queued_s"] for r in res]
     for h in hams:
         h.close()
@@ -350,7 +351,11 @@ def batch_workload(a):
             "data": "synthetic", "status": st, "one_at_a_time": round(k / t_seq, 3),
             "speedup_vs_one_at_a_time": round((a.problems / t_bat) / (k / t_seq), 3),
             "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99), "same_alone_and_in_batch": same,
+            "max_dE_alone_vs_batch_Ha": dE_alone,
             "converged": int(sum(r["converged"] for r in res)), "build_s": round(t_build, 2),
+            "iterations_fp32_mean": float(np.mean([r["iterations_fp32"] for r in res])),
+            "iterations_fp64_mean": float(np.mean([r["iterations"] - r["iterations_fp32"] for r in res])),
+            "iterations_max": int(max(r["iterations"] for r in res)),
             "autotune_s": round(t_tune, 2), "tile_dets_per_thread": {str(k): v for k, v in sorted(tuned.items())},
             "config": {"workload": f"{a.problems} Hamiltonians, L uniform in {lmin}..{lmax}, N=L//2, "
                                    f"{a.roots} roots", "opts": opts,

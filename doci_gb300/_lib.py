@@ -222,8 +222,9 @@ class Hamiltonian:
         self.close()
 
     def engine_autotune(self, nvec: int = 1) -> int:
-        """The batch engine's sigma tile (determinants per thread) for this
-        shape, timed and kept for the process; doci_engine_autotune."""
+        """The batch engine's sigma path for this shape, timed and kept for
+        the process: 1, 2 or 4 determinants per thread of the batched gather,
+        or 0 for the single-problem kernels; doci_engine_autotune."""
         d = C.c_int()
         _check(lib().doci_engine_autotune(self._h, int(nvec), C.byref(d)), "doci_engine_autotune")
         return d.value

@@ -22,8 +22,13 @@
 // on the other problems of the batch: a problem's determinants and vector
 // chunks are the same whatever else runs, every reduction finishes in a fixed
 // order (per-chunk partial rows summed by the problem's last chunk to
-// finish), and sigma has no atomics -- so a result is bit-identical alone and
-// in any batch.  Mixed mode: an FP32 phase on H - s (s = the lowest diagonal
+// finish), and the batched sigma has no atomics -- so a result is
+// bit-identical alone and in any batch.  Large problems (from 2^22
+// determinants, or as the shape's autotuning decides) take their sigmas from
+// the single-problem kernels (launch_sigma: the pair form for FP32) on
+// staging buffers instead; their results still do not depend on the batch,
+// but the FP32 pair form's atomic adds make their last bits vary from run to
+// run.  Mixed mode: an FP32 phase on H - s (s = the lowest diagonal
 // element; FP32 basis, sigma and vector arithmetic with FP64 sums), ending at
 // mixed_tol or when the largest residual has not reached a new minimum for
 // 15 iterations, then the FP64 phase from its Ritz vectors.
@@ -33,6 +38,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <tuple>
 #include <vector>
@@ -159,6 +165,7 @@ __global__ void __launch_bounds__(kET) eng_sigma(EArgs a) {
   __shared__ uint32_t B[kBinomRows * kBinomCols];
   for (int t = threadIdx.x; t < kBinomRows * kBinomCols; t += kET) B[t] = a.binom[t];
   __syncthreads();
+  if (blockIdx.x >= __ldg(a.tile0 + a.n)) return;
   const int p = owner(a.tile0, a.n, blockIdx.x);
   const EProb &pb = a.P[p];
   const EState &st = a.St[p];
@@ -396,6 +403,22 @@ __global__ void __launch_bounds__(kET) eng_combine(EArgs a) {
         if (k < m) s += static_cast<double>(V[static_cast<size_t>(k) * pb.D + jj]) * st.Y[r * kMaxV + k];
       pb.X[static_cast<size_t>(r) * pb.D + jj] = s;
     }
+  }
+}
+
+// large problems take their sigmas from the single-problem kernels
+// (launch_sigma) on fixed staging buffers: the new basis vectors are copied in
+// (xs[v] = V[:, m0 + v], v < m - m0) and the sigmas out (VA[:, m0 + v] = ys[v])
+template <typename S>
+__global__ void eng_stage(EArgs a, int p, S *xs, const S *ys, int out) {
+  const EProb &pb = a.P[p];
+  const EState &st = a.St[p];
+  if (st.done) return;
+  const int m0 = st.m0, nv = st.m - st.m0;
+  const size_t n = static_cast<size_t>(nv > 0 ? nv : 0) * pb.D;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (out) static_cast<S *>(pb.VA)[static_cast<size_t>(m0) * pb.D + i] = ys[i];
+    else xs[i] = static_cast<const S *>(pb.V)[static_cast<size_t>(m0) * pb.D + i];
   }
 }
 
@@ -665,9 +688,21 @@ struct DBuf {
 
 inline unsigned nblk(uint64_t n) { return static_cast<unsigned>(n < 1 ? 1 : n); }
 
+// a problem whose sigmas come from launch_sigma (its handle, or the FP32
+// phase's shifted view of it) through staging buffers of R vectors
+struct BigProb {
+  int p;
+  const doci_ham *h;
+  void *xs, *ys;
+  size_t D;
+};
+
 template <typename S, int KM, int NH>
-int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool unit_start) {
+int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool unit_start,
+              const std::vector<BigProb> &big) {
   const int n = a.n, R = a.R;
+  const int prec = sizeof(S) == 8 ? DOCI_FP64 : DOCI_FP32;
+  std::vector<char> big_running(big.size(), 1);
   const unsigned small = (n + 127) / 128;
   eng_init_state<<<small, 128, 0, st>>>(a);
   if (unit_start) {
@@ -687,32 +722,55 @@ int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool
       eng_gs_finish<S><<<nblk(nchunks), kET, 0, st>>>(a, q);
       eng_orth_commit<<<small, 128, 0, st>>>(a, q, q == R - 1);
     }
-    eng_sigma<S, NH><<<nblk(ntiles), kET, 0, st>>>(a);
+    if (ntiles > 0) eng_sigma<S, NH><<<nblk(ntiles), kET, 0, st>>>(a);
+    for (size_t b = 0; b < big.size(); ++b) {
+      if (!big_running[b]) continue;
+      const BigProb &bp = big[b];
+      eng_stage<S><<<nblk(std::min<uint64_t>((bp.D * R + 255) / 256, 4096)), 256, 0, st>>>(
+          a, bp.p, static_cast<S *>(bp.xs), nullptr, 0);
+      for (int v = 0; v < R; ++v) {
+        const int sv = launch_sigma(bp.h, static_cast<S *>(bp.xs) + v * bp.D, static_cast<S *>(bp.ys) + v * bp.D,
+                                    prec, st);
+        if (sv) return sv;
+      }
+      eng_stage<S><<<nblk(std::min<uint64_t>((bp.D * R + 255) / 256, 4096)), 256, 0, st>>>(
+          a, bp.p, nullptr, static_cast<const S *>(bp.ys), 1);
+    }
     for (int j = 0; j < R; ++j) eng_subcol<S, KM><<<nblk(nchunks), kET, 0, st>>>(a, j);
     DOCI_CUDA(cudaGetLastError());
     return DOCI_OK;
   };
   int s = extend();
   if (s) return s;
-  // one iteration, captured once and replayed
-  cudaGraph_t graph = nullptr;
+  // one iteration, captured and replayed (captured again when a large
+  // problem finishes, so that its sigmas are no longer launched)
   cudaGraphExec_t exec = nullptr;
-  DOCI_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  eng_eig<<<n, 32, 0, st>>>(a);
-  eng_deflate<S, KM><<<nblk(nchunks), kET, 0, st>>>(a);
-  eng_after_restart<<<small, 128, 0, st>>>(a);
-  for (int q = 0; q < R; ++q) eng_residual<S, KM><<<nblk(nchunks), kET, 0, st>>>(a, q);
-  eng_control<<<small, 128, 0, st>>>(a);
-  s = extend();
-  cudaError_t ce = cudaStreamEndCapture(st, &graph);
-  if (s) {
-    if (graph) cudaGraphDestroy(graph);
-    return s;
-  }
-  DOCI_CUDA(ce);
-  ce = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
-  DOCI_CUDA(ce);
+  auto capture = [&]() -> int {
+    if (exec) {
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    DOCI_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    eng_eig<<<n, 32, 0, st>>>(a);
+    eng_deflate<S, KM><<<nblk(nchunks), kET, 0, st>>>(a);
+    eng_after_restart<<<small, 128, 0, st>>>(a);
+    for (int q = 0; q < R; ++q) eng_residual<S, KM><<<nblk(nchunks), kET, 0, st>>>(a, q);
+    eng_control<<<small, 128, 0, st>>>(a);
+    const int se = extend();
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (se) {
+      if (graph) cudaGraphDestroy(graph);
+      return se;
+    }
+    DOCI_CUDA(ce);
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    DOCI_CUDA(ce);
+    return DOCI_OK;
+  };
+  s = capture();
+  if (s) return s;
   std::vector<int> flags(n);
   int status = DOCI_OK;
   for (int it = 0; it <= a.max_its + 1; ++it) {
@@ -724,8 +782,15 @@ int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool
       break;
     }
     if (std::none_of(flags.begin(), flags.end(), [](int f) { return f != 0; })) break;
+    bool changed = false;
+    for (size_t b = 0; b < big.size(); ++b)
+      if (big_running[b] && !flags[big[b].p]) {
+        big_running[b] = 0;
+        changed = true;
+      }
+    if (changed && (status = capture())) break;
   }
-  cudaGraphExecDestroy(exec);
+  if (exec) cudaGraphExecDestroy(exec);
   if (status) return status;
   eng_combine<S, KM><<<nblk(nchunks), kET, 0, st>>>(a);
   DOCI_CUDA(cudaGetLastError());
@@ -733,18 +798,20 @@ int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool
 }
 
 template <typename S, int KM>
-int run_phase_nh(EArgs &a, int nh_max, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool unit_start) {
-  if (nh_max <= 8) return run_phase<S, KM, 8>(a, ntiles, nchunks, st, unit_start);
-  if (nh_max <= 16) return run_phase<S, KM, 16>(a, ntiles, nchunks, st, unit_start);
-  if (nh_max <= 24) return run_phase<S, KM, 24>(a, ntiles, nchunks, st, unit_start);
-  return run_phase<S, KM, 32>(a, ntiles, nchunks, st, unit_start);
+int run_phase_nh(EArgs &a, int nh_max, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool unit_start,
+                 const std::vector<BigProb> &big) {
+  if (nh_max <= 8) return run_phase<S, KM, 8>(a, ntiles, nchunks, st, unit_start, big);
+  if (nh_max <= 16) return run_phase<S, KM, 16>(a, ntiles, nchunks, st, unit_start, big);
+  if (nh_max <= 24) return run_phase<S, KM, 24>(a, ntiles, nchunks, st, unit_start, big);
+  return run_phase<S, KM, 32>(a, ntiles, nchunks, st, unit_start, big);
 }
 
 template <typename S>
-int run_phase_km(EArgs &a, int nh_max, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool unit_start) {
-  if (a.maxv <= 8) return run_phase_nh<S, 8>(a, nh_max, ntiles, nchunks, st, unit_start);
-  if (a.maxv <= 16) return run_phase_nh<S, 16>(a, nh_max, ntiles, nchunks, st, unit_start);
-  return run_phase_nh<S, 32>(a, nh_max, ntiles, nchunks, st, unit_start);
+int run_phase_km(EArgs &a, int nh_max, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool unit_start,
+                 const std::vector<BigProb> &big) {
+  if (a.maxv <= 8) return run_phase_nh<S, 8>(a, nh_max, ntiles, nchunks, st, unit_start, big);
+  if (a.maxv <= 16) return run_phase_nh<S, 16>(a, nh_max, ntiles, nchunks, st, unit_start, big);
+  return run_phase_nh<S, 32>(a, nh_max, ntiles, nchunks, st, unit_start, big);
 }
 
 __global__ void shifted_diag32_kernel(const double *d, double shift, float *out, uint32_t n) {
@@ -752,14 +819,24 @@ __global__ void shifted_diag32_kernel(const double *d, double shift, float *out,
     out[i] = static_cast<float>(d[i] - shift);
 }
 
-// sigma tile shape per (device, L, N): determinants per thread (1, 2 or 4)
+// sigma choice per (device, L, N): the tile shape of the batched pass
+// (determinants per thread: 1, 2 or 4) and whether the problem's sigmas come
+// from the single-problem kernels instead (untuned: from 2^22 determinants,
+// where those kernels' row tilings beat the per-determinant gather)
+struct TileChoice {
+  int dpt = 1;
+  int kernels = -1;  // -1 untuned
+};
 std::mutex g_tile_mu;
-std::map<std::tuple<int, int, int>, int> g_tile;
+std::map<std::tuple<int, int, int>, TileChoice> g_tile;
+constexpr uint32_t kBigD = 1u << 22;
 
-int tile_dpt(const doci_ham *h) {
+TileChoice tile_choice(const doci_ham *h) {
   std::lock_guard<std::mutex> lk(g_tile_mu);
   auto it = g_tile.find(std::make_tuple(h->device, h->L, h->N));
-  return it == g_tile.end() ? 1 : it->second;
+  TileChoice c = it == g_tile.end() ? TileChoice{} : it->second;
+  if (c.kernels < 0) c.kernels = h->D >= kBigD ? 1 : 0;
+  return c;
 }
 
 __global__ void eng_tune_state(EState *st, int nv) {
@@ -838,14 +915,32 @@ int engine_tune(doci_ham *h, int nv, int *dpt_out) {
       best = dpt;
     }
   }
+  // the single-problem kernels on the same vectors, one sigma per vector
+  int kernels = 0;
+  {
+    bool ok = true;
+    for (int k = 0; k < 4 && ok; ++k) {  // warm-up, then three timed rounds
+      if (k == 1) cudaEventRecord(e0, st);
+      for (int v = 0; v < nv && ok; ++v)
+        ok = launch_sigma(h, V.p + static_cast<size_t>(v) * D, VA.p + static_cast<size_t>(v) * D, DOCI_FP32, st) ==
+             DOCI_OK;
+    }
+    cudaEventRecord(e1, st);
+    float ms = 1e30f;
+    if (ok && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    kernels = ms < best_ms ? 1 : 0;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   DOCI_CUDA(cudaGetLastError());
   {
     std::lock_guard<std::mutex> lk(g_tile_mu);
-    g_tile[std::make_tuple(h->device, h->L, h->N)] = best;
+    TileChoice c;
+    c.dpt = best;
+    c.kernels = kernels;
+    g_tile[std::make_tuple(h->device, h->L, h->N)] = c;
   }
-  if (dpt_out) *dpt_out = best;
+  if (dpt_out) *dpt_out = kernels ? 0 : best;
   return DOCI_OK;
 }
 
@@ -856,8 +951,8 @@ int64_t engine_footprint(int L, int N, const doci_batch_opts &o) {
   const int64_t mv = std::min(kMaxV, std::max(o.max_vec, 2 * o.nroots));
   const int64_t ham = D * 12 + (16ll << 20);  // the handle's diagonals and tables
   const int64_t x = D * R * 8;                 // Ritz vectors
-  const int64_t p64 = 2 * mv * D * 8 + R * D * 8;
-  const int64_t p32 = o.mode == DOCI_MODE_MIXED ? 2 * mv * D * 4 + R * D * 4 + D * 4 : 0;
+  const int64_t p64 = 2 * mv * D * 8 + R * D * 8 + 2 * R * D * 8;  // + staging of a large problem
+  const int64_t p32 = o.mode == DOCI_MODE_MIXED ? 2 * mv * D * 4 + R * D * 4 + D * 4 + 2 * R * D * 4 : 0;
   return ham + x + p64 + p32 + (1ll << 20);
 }
 
@@ -878,14 +973,16 @@ int engine_solve(int n, doci_ham *const *hams, const doci_batch_opts &o, cudaStr
   if (a.keep > a.maxv - R) a.keep = a.maxv - R;
   a.tol = o.tol;
   std::vector<uint32_t> tile0(n + 1, 0), chunk0(n + 1, 0);
-  std::vector<int> dpt(n, 1);
+  std::vector<int> dpt(n, 1), big_idx;
   size_t total = 0;
   int nh_max = 1;
   for (int i = 0; i < n; ++i) {
     const doci_ham *h = hams[i];
     if (!h || static_cast<int64_t>(h->D) < 1) return DOCI_ERR_INVALID;
-    dpt[i] = tile_dpt(h);
-    tile0[i + 1] = tile0[i] + static_cast<uint32_t>((h->D + kET * dpt[i] - 1) / (kET * dpt[i]));
+    const TileChoice tc = tile_choice(h);
+    dpt[i] = tc.dpt;
+    if (tc.kernels) big_idx.push_back(i);
+    tile0[i + 1] = tile0[i] + (tc.kernels ? 0u : static_cast<uint32_t>((h->D + kET * dpt[i] - 1) / (kET * dpt[i])));
     chunk0[i + 1] = chunk0[i] + (h->D + kEChunk - 1) / kEChunk;
     total += h->D;
     nh_max = std::max(nh_max, h->nh);
@@ -977,13 +1074,26 @@ int engine_solve(int n, doci_ham *const *hams, const doci_batch_opts &o, cudaStr
       DOCI_CUDA(cudaGetLastError());
       if ((s = upload())) return s;
     }
+    // large problems: shifted views (FP32 diagonal - shift) and staging
+    std::vector<std::unique_ptr<doci_ham>> views;
+    std::vector<std::unique_ptr<DBuf<float>>> stg;
+    std::vector<BigProb> big;
+    for (int i : big_idx) {
+      views.emplace_back(new doci_ham(*hams[i]));
+      views.back()->d_diag32 = static_cast<float *>(const_cast<void *>(P[i].diag_s));
+      views.back()->sigma_kernel = hams[i]->sigma_kernel;
+      stg.emplace_back(new DBuf<float>());
+      if ((s = stg.back()->alloc(2 * static_cast<size_t>(hams[i]->D) * R, st))) return s;
+      big.push_back(BigProb{i, views.back().get(), stg.back()->p, stg.back()->p + static_cast<size_t>(hams[i]->D) * R,
+                            hams[i]->D});
+    }
     EArgs a32 = a;
     a32.tol = o.mixed_tol > o.tol ? o.mixed_tol : o.tol;
     a32.stall_window = 15;
     a32.max_its = o.max_its;
     for (int i = 0; i < n; ++i) P[i].max_its = o.max_its;
     if ((s = upload())) return s;
-    s = run_phase_km<float>(a32, nh_max, ntiles, nchunks, st, true);
+    s = run_phase_km<float>(a32, nh_max, ntiles, nchunks, st, true, big);
     if (s) return s;
     DOCI_CUDA(cudaMemcpyAsync(host_st.data(), dS.p, sizeof(EState) * n, cudaMemcpyDeviceToHost, st));
     DOCI_CUDA(cudaStreamSynchronize(st));
@@ -1017,7 +1127,15 @@ int engine_solve(int n, doci_ham *const *hams, const doci_batch_opts &o, cudaStr
     }
     if ((s = upload())) return s;
     a64.max_its = max64;
-    s = run_phase_km<double>(a64, nh_max, ntiles, nchunks, st, !have_start);
+    std::vector<std::unique_ptr<DBuf<double>>> stg;
+    std::vector<BigProb> big;
+    for (int i : big_idx) {
+      stg.emplace_back(new DBuf<double>());
+      if ((s = stg.back()->alloc(2 * static_cast<size_t>(hams[i]->D) * R, st))) return s;
+      big.push_back(BigProb{i, hams[i], stg.back()->p, stg.back()->p + static_cast<size_t>(hams[i]->D) * R,
+                            hams[i]->D});
+    }
+    s = run_phase_km<double>(a64, nh_max, ntiles, nchunks, st, !have_start, big);
     if (s) return s;
     DOCI_CUDA(cudaMemcpyAsync(host_st.data(), dS.p, sizeof(EState) * n, cudaMemcpyDeviceToHost, st));
     DOCI_CUDA(cudaStreamSynchronize(st));

@@ -350,21 +350,27 @@ int64_t doci_roots_footprint(int L, int n_pairs, const doci_batch_opts *opts);
  * be NULL. */
 int doci_solve_roots(doci_ham *ham, const doci_batch_opts *opts, doci_root_result *result, double *vecs);
 
-/* Tile autotuning of the batch engine: time its sigma's tile shapes (1, 2 or
- * 4 determinants per thread of a 256-thread tile) on this handle with nvec
- * (1..8) vectors and keep the fastest for every problem of the same
- * (device, L, n_pairs) in the process; *dets_per_thread receives it (may be
- * NULL).  Changes no result (each determinant's sum is the same in every
- * tile shape).  Synchronous.  No counterpart in the reference. */
+/* Autotuning of the batch engine's sigma for this handle's shape: time its
+ * batched gather with tiles of 1, 2 or 4 determinants per thread of a
+ * 256-thread tile, and the single-problem kernels (doci_sigma's path, one
+ * call per vector), on nvec (1..8) vectors; keep the fastest for every
+ * problem of the same (device, L, n_pairs) in the process.
+ * *dets_per_thread (may be NULL) receives the tile, or 0 for the
+ * single-problem kernels.  Untuned shapes use one determinant per thread
+ * below 2^22 determinants and the single-problem kernels from there.  A tile
+ * shape changes no result; the single-problem kernels reduce in another
+ * order.  Synchronous.  No counterpart in the reference. */
 int doci_engine_autotune(doci_ham *ham, int nvec, int *dets_per_thread);
 
 /* Solve many Hamiltonians at once on the batch engine: every problem of a
  * group advances in lockstep, one device-resident, graph-captured block
  * Davidson iteration for the whole group (batched sigma over a shared space
- * of determinant tiles, batched vector passes, one subspace eigensolver per
- * problem on the device); groups are formed in order so that their solves
- * fit opts->hbm_budget (0: 85% of the free memory).  A result does not
- * depend on the rest of the batch.  results[i] for hams[i] (start_s / end_s:
+ * of determinant tiles -- large problems take doci_sigma's kernels instead,
+ * see doci_engine_autotune -- batched vector passes, one subspace
+ * eigensolver per problem on the device); groups are formed in order so
+ * that their solves fit opts->hbm_budget (0: 85% of the free memory).  A
+ * result does not depend on the rest of the batch (bit for bit on the
+ * batched path).  results[i] for hams[i] (start_s / end_s:
  * the group's run, seconds from the call). */
 int doci_batch_solve(int n, doci_ham *const *hams, const doci_batch_opts *opts, doci_root_result *results);
 

@@ -106,3 +106,20 @@ def test_server_admission_rejects_oversized(dg):
         t = srv.submit(12, 6, one, two)
         r = srv.wait(t)
     assert r["status"] == 9  # DOCI_ERR_ADMISSION
+
+
+def test_engine_tile_autotune(synth, dg):
+    """doci_engine_autotune picks, for one (L, N) shape, the batch engine's
+    sigma path: a tile of 1, 2 or 4 determinants per thread of the batched
+    gather (returned as 1, 2, 4), or the single-problem kernels (returned as
+    0).  A tile shape changes which thread computes a determinant, not its
+    sum; the single-problem kernels reduce in another order.  Either way the
+    solve reaches the same energies, within the residual tolerance's
+    quadratic energy error."""
+    with dg.Hamiltonian.from_fcidump(synth(16, 8, 61)) as h:
+        before = dg.solve_roots(h, nroots=2, tol=1e-6, mode="mixed")
+        choice = h.engine_autotune(2)
+        assert choice in (0, 1, 2, 4)
+        after = dg.solve_roots(h, nroots=2, tol=1e-6, mode="mixed")
+    assert before["converged"] == after["converged"] == 1
+    assert np.allclose(before["energies"], after["energies"], rtol=0, atol=1e-9)
