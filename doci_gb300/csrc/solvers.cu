@@ -113,34 +113,6 @@ int MatvecOp::apply(const void *d_x, void *d_y, int precision, cudaStream_t st) 
   return DOCI_OK;
 }
 
-int MatvecOp::apply_multi(const void *d_x, size_t ldx, void *d_y, size_t ldy, int nv, int precision,
-                          cudaStream_t st) {
-  const size_t es = precision == DOCI_FP64 ? 8 : 4;
-  if (!ham) {
-    for (int v = 0; v < nv; ++v) {
-      const int s = apply(static_cast<const char *>(d_x) + v * ldx * es, static_cast<char *>(d_y) + v * ldy * es,
-                          precision, st);
-      if (s != DOCI_OK) return s;
-    }
-    return DOCI_OK;
-  }
-  if (events_on) cudaEventRecord(ev0, st);
-  int s = DOCI_OK;
-  for (int v0 = 0; v0 < nv && s == DOCI_OK; v0 += 4) {
-    const int k = nv - v0 < 4 ? nv - v0 : 4;
-    s = launch_sigma_multi(ham, static_cast<const char *>(d_x) + v0 * ldx * es, ldx,
-                           static_cast<char *>(d_y) + v0 * ldy * es, ldy, k, precision, st);
-  }
-  if (events_on) {
-    cudaEventRecord(ev1, st);
-    cudaEventSynchronize(ev1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ev0, ev1);
-    sigma_seconds += ms * 1e-3;
-  }
-  return s;
-}
-
 void MatvecOp::enable_timing() {
   if (!events_on && ham) {
     cudaEventCreate(&ev0);
@@ -322,165 +294,6 @@ template int davidson_run<double>(MatvecOp &, size_t, const double *, double *, 
 template int davidson_run<float>(MatvecOp &, size_t, const double *, float *, const DavidsonArgs &, cudaStream_t,
                                  DavidsonOut *, double *);
 
-
-// ---------------------------------------------------------------------------
-// Block Davidson (nroots lowest eigenpairs).  Each iteration appends the
-// preconditioned residuals of the unconverged roots, each orthogonalised by
-// classical Gram-Schmidt twice against the whole basis (skipped if it has no
-// component left), computes their sigmas in one multi-vector pass and the new
-// subspace columns, and
-// re-diagonalises; the basis restarts from the `keep` lowest Ritz vectors
-// when the next block would not fit.
-// ---------------------------------------------------------------------------
-template <typename S>
-int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, const BlockArgs &a, cudaStream_t st,
-                       BlockOut *out, double *d_X_out) {
-  const int R = a.nroots, maxv = a.max_vectors;
-  const int keep = a.keep > R ? a.keep : R;
-  if (R < 1 || R > 8 || maxv > 32 || maxv < keep + R) return DOCI_ERR_INVALID;
-  const int precision = sizeof(S) == 8 ? DOCI_FP64 : DOCI_FP32;
-  DevMem V, VA, part, small, tbuf;
-  DOCI_TRY(V.alloc(sizeof(S) * D * maxv, st));
-  DOCI_TRY(VA.alloc(sizeof(S) * D * maxv, st));
-  DOCI_TRY(tbuf.alloc(sizeof(S) * D * R, st));
-  DOCI_TRY(part.alloc(sizeof(double) * vec_partials_capacity(), st));
-  DOCI_TRY(vec_partials_init(part.as<double>(), st));
-  DOCI_TRY(small.alloc(sizeof(double) * (96 + 32 * 32), st));
-  double *d_red = small.as<double>(), *d_vec = d_red + 64, *d_Y = d_red + 96;
-  S *Vp = V.as<S>(), *VAp = VA.as<S>(), *Tp = tbuf.as<S>();
-  double *dp = part.as<double>();
-  std::vector<double> Sm(maxv * maxv, 0.0), Y(maxv * maxv, 0.0), w(maxv, 0.0), red(64);
-  auto fetch = [&](int nk) -> int {
-    DOCI_CUDA(cudaMemcpyAsync(red.data(), vec_results(dp), sizeof(double) * nk, cudaMemcpyDeviceToHost, st));
-    DOCI_CUDA(cudaStreamSynchronize(st));
-    return DOCI_OK;
-  };
-  // orthonormalise the vector in `t` against V_0..V_{m-1} into V_m (no
-  // sigma yet); `added` is false when nothing independent is left
-  int m = 0;
-  auto orth = [&](S *t, bool *added) -> int {
-    *added = false;
-    double n0;
-    DOCI_TRY(vec_multidot<S>(t, D, 1, t, D, dp, st));
-    DOCI_TRY(fetch(1));
-    n0 = red[0];
-    if (!(n0 > 0)) return DOCI_OK;
-    std::vector<double> c(32, 0.0);
-    if (m > 0) {
-      for (int pass = 0; pass < 2; ++pass) {
-        DOCI_TRY(vec_multidot<S>(Vp, D, m, t, D, dp, st));
-        DOCI_TRY(fetch(m));
-        for (int i = 0; i < m; ++i) c[i] = red[i];
-        DOCI_CUDA(cudaMemcpyAsync(d_vec, c.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
-        DOCI_TRY(vec_gs_update<S>(Vp, D, m, d_vec, D, t, dp, st));
-      }
-      DOCI_TRY(fetch(m + 1));
-    } else {
-      red[0] = n0;
-    }
-    const double n1 = red[0];
-    if (!(n1 > 1e-20 * n0) || !(n1 > 0)) return DOCI_OK;  // no independent direction left
-    DOCI_TRY(vec_gs_finish<S>(Vp, D, 0, nullptr, 1.0 / std::sqrt(n1), D, t, Vp + static_cast<size_t>(m) * D, dp, st));
-    ++m;
-    *added = true;
-    return DOCI_OK;
-  };
-  // sigmas of the new basis vectors V_m0..V_{m-1} in one multi-vector pass,
-  // then their subspace columns
-  auto extend = [&](int m0) -> int {
-    if (m == m0) return DOCI_OK;
-    DOCI_TRY(op.apply_multi(Vp + static_cast<size_t>(m0) * D, D, VAp + static_cast<size_t>(m0) * D, D, m - m0,
-                            precision, st));
-    out->sigmas += m - m0;
-    for (int i = m0; i < m; ++i) {
-      DOCI_TRY(vec_multidot<S>(Vp, D, i + 1, VAp + static_cast<size_t>(i) * D, D, dp, st));
-      DOCI_TRY(fetch(i + 1));
-      for (int k = 0; k <= i; ++k) Sm[i * maxv + k] = red[k];
-    }
-    return DOCI_OK;
-  };
-
-  std::vector<int> active(R, 1);
-  std::vector<double> res(R, 1e300);
-  double best = 1e300;
-  int stall = 0, its = 0;
-  // start block
-  for (int r = 0; r < R; ++r) {
-    bool added;
-    DOCI_TRY(orth(d_T + static_cast<size_t>(r) * D, &added));
-  }
-  if (m == 0) return DOCI_ERR_INVALID;
-  DOCI_TRY(extend(0));
-  while (true) {
-    ++its;
-    jacobi_eig(m, Sm.data(), maxv, w.data(), Y.data());
-    const int nr = R < m ? R : m;
-    if (m + R > maxv) {  // thick restart to the `keep` lowest Ritz vectors
-      const int kk = keep < m ? keep : m;
-      DOCI_CUDA(cudaMemcpyAsync(d_Y, Y.data(), sizeof(double) * maxv * kk, cudaMemcpyHostToDevice, st));
-      DOCI_TRY(vec_deflate<S>(Vp, D, m, kk, d_Y, maxv, D, st));
-      DOCI_TRY(vec_deflate<S>(VAp, D, m, kk, d_Y, maxv, D, st));
-      for (int cc = 0; cc < kk; ++cc) {
-        DOCI_TRY(vec_multidot<S>(Vp, D, cc + 1, VAp + static_cast<size_t>(cc) * D, D, dp, st));
-        DOCI_TRY(fetch(cc + 1));
-        for (int i = 0; i <= cc; ++i) Sm[cc * maxv + i] = red[i];
-      }
-      m = kk;
-      jacobi_eig(m, Sm.data(), maxv, w.data(), Y.data());
-    }
-    // residuals and corrections of the unconverged roots
-    double worst = 0;
-    int nnew = 0;
-    for (int r = 0; r < nr; ++r) {
-      DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data() + static_cast<size_t>(r) * maxv, sizeof(double) * m,
-                                cudaMemcpyHostToDevice, st));
-      S *t = Tp + static_cast<size_t>(nnew) * D;
-      DOCI_TRY(vec_residual<S>(Vp, VAp, D, m, d_vec, w[r], d_diag, D, t, nullptr, dp, st, a.shift));
-      DOCI_TRY(fetch(m + 2));  // the residual pass writes m + 2 partials per block
-      res[r] = std::sqrt(red[0]);
-      worst = res[r] > worst ? res[r] : worst;
-      active[r] = res[r] > a.tol;
-      if (active[r]) ++nnew;
-    }
-    out->iterations = its;
-    if (worst <= a.tol || its >= a.max_its) break;
-    if (a.stall_window > 0) {
-      if (worst < best) {
-        best = worst;
-        stall = 0;
-      } else if (++stall >= a.stall_window) {
-        break;
-      }
-    }
-    const int m0 = m;
-    for (int q = 0; q < nnew; ++q) {
-      bool added;
-      DOCI_TRY(orth(Tp + static_cast<size_t>(q) * D, &added));
-    }
-    if (m == m0) break;
-    DOCI_TRY(extend(m0));
-  }
-  const int nr = R < m ? R : m;
-  for (int r = 0; r < nr; ++r) {
-    out->energy[r] = w[r] + a.shift;
-    out->residual[r] = res[r];
-    if (d_X_out) {
-      DOCI_CUDA(cudaMemcpyAsync(d_vec, Y.data() + static_cast<size_t>(r) * maxv, sizeof(double) * m,
-                                cudaMemcpyHostToDevice, st));
-      DOCI_TRY(vec_combine<S>(Vp, D, m, d_vec, D, d_X_out + static_cast<size_t>(r) * D, st));
-    }
-  }
-  double worst = 0;
-  for (int r = 0; r < nr; ++r) worst = res[r] > worst ? res[r] : worst;
-  out->converged = worst <= a.tol;
-  DOCI_CUDA(cudaStreamSynchronize(st));
-  return DOCI_OK;
-}
-
-template int block_davidson_run<double>(MatvecOp &, size_t, const double *, double *, const BlockArgs &, cudaStream_t,
-                                        BlockOut *, double *);
-template int block_davidson_run<float>(MatvecOp &, size_t, const double *, float *, const BlockArgs &, cudaStream_t,
-                                       BlockOut *, double *);
 
 // RQ-CG (CG.c:13-164).  d_x holds the start vector and receives the result.
 int ray_q_run(MatvecOp &op, size_t D, const double *d_diag_or_null, double *d_x, const CgArgs &a, cudaStream_t st,

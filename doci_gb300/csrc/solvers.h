@@ -36,9 +36,6 @@ struct MatvecOp {
   float *x32 = nullptr, *y32 = nullptr;  // D-element scratch, owned by the caller
   bool anchor_next = true;
   int apply(const void *d_x, void *d_y, int precision, cudaStream_t st);
-  // nv vectors x + v ldx -> y + v ldy (consecutive columns); the device sigma
-  // shares its neighbour work over up to four vectors per launch
-  int apply_multi(const void *d_x, size_t ldx, void *d_y, size_t ldy, int nv, int precision, cudaStream_t st);
   void enable_timing();
   ~MatvecOp();
 };
@@ -97,27 +94,6 @@ struct ShiftedView {
   ShiftedView &operator=(const ShiftedView &) = delete;
   ~ShiftedView();
 };
-
-struct BlockArgs {
-  int nroots = 1, max_vectors = 16, keep = 0, max_its = 200;
-  double tol = 1e-8;         // on every root's residual norm
-  int stall_window = 0;      // > 0: stop when the largest residual stops reaching new minima
-  double shift = 0;          // the operator is H - shift, as in DavidsonArgs
-};
-
-struct BlockOut {
-  double energy[8] = {};
-  double residual[8] = {};
-  int iterations = 0, converged = 0, sigmas = 0;
-};
-
-// Block Davidson for the nroots lowest eigenpairs (no counterpart in the
-// reference, which is single-root).  d_T holds nroots start vectors (column-
-// major D x nroots, storage S); d_X_out (FP64, D x nroots) receives the Ritz
-// vectors.  diag is the FP64 diagonal (preconditioner |diag - theta|).
-template <typename S>
-int block_davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_T, const BlockArgs &a, cudaStream_t st,
-                       BlockOut *out, double *d_X_out);
 
 template <typename S>
 int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const DavidsonArgs &a, cudaStream_t st,
