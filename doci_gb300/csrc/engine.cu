@@ -143,11 +143,15 @@ __device__ bool chunk_reduce(const double (&acc)[NK], int nk, const EArgs &a, co
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  if (threadIdx.x < nk) {
+  // one warp per output, lanes over the rows (stride 32), then a fixed
+  // shuffle tree: the order depends only on the problem's chunk count
+  const double *r0 = a.part + static_cast<size_t>(pb.chunk0) * kLdp;
+  for (int k = warp; k < nk; k += kET / 32) {
     double s = 0;
-    const double *r0 = a.part + static_cast<size_t>(pb.chunk0) * kLdp + threadIdx.x;
-    for (uint32_t c = 0; c < pb.nchunks; ++c) s += __ldcg(r0 + static_cast<size_t>(c) * kLdp);
-    out[threadIdx.x] = s;
+    for (uint32_t c = lane; c < pb.nchunks; c += 32) s += __ldcg(r0 + static_cast<size_t>(c) * kLdp + k);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) out[k] = s;
   }
   if (threadIdx.x == 0) a.cnt[p] = 0;
   __syncthreads();

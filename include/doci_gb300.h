@@ -170,9 +170,9 @@ int doci_sigma(doci_ham *ham, const void *d_x, void *d_y, int precision, void *s
 int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int64_t ldy, int nv, int precision,
                      void *stream);
 
-/* Sigma kernel selection for a handle: 0 automatic (default: for FP32 with a
- * row tiling that gives every SM work, kind 6; else with a row tiling kind 3
- * for FP32 and kind 4 for FP64; else kind 1),
+/* Sigma kernel selection for a handle: 0 automatic (default: with a row
+ * tiling that gives every SM work, kind 6 for FP32 and kind 9 for FP64; else
+ * with a row tiling kind 3 for FP32 and kind 4 for FP64; else kind 1),
  * 1 the per-determinant gather kernel, 3 the row pass doing all hops, 4 the
  * phase-ordered row pass (cross hops staged one source row at a time), 6 the
  * (N-1)-pair form on the warp-level tensor-core path (FP32 only: gather the
@@ -180,10 +180,12 @@ int doci_sigma_block(doci_ham *ham, const void *d_X, int64_t ldx, void *d_Y, int
  * adds), 8 the (N-1)-pair form on the 5th-generation tensor cores (FP32
  * only: the own row of a set's row part staged in shared memory, the other
  * rows streamed by TMA, the product in TMEM, each own row written once;
- * needs a 16-byte aligned x, else kind 6 runs), 9 the phase-ordered row
- * pass in float-float arithmetic (FP64 only: FP64 accuracy from pairs of
- * FP32 values, x converted once per call into stream-ordered scratch of D x 8
- * bytes; FP32 requests for it use the automatic choice).  Kinds 6 and 8 reduce into
+ * needs a 16-byte aligned x, else kind 6 runs), 9 the (N-1)-pair form in
+ * float-float arithmetic (FP64 only: FP64 accuracy from pairs of FP32
+ * values on the FP32 units, x converted once per call into stream-ordered
+ * scratch of D x 8 bytes, FP64 atomic adds into sigma; the phase-ordered row
+ * pass in the same arithmetic where the pair tiling does not fit; FP32
+ * requests for it use the automatic choice).  Kinds 6, 8 and 9 reduce into
  * sigma with atomic adds, so their last bits vary between runs; FP64
  * requests for them use the automatic choice.  3-9 fall back to 1 when the
  * handle has no row tiling.  Other values: DOCI_ERR_INVALID.  A device wait

@@ -243,8 +243,9 @@ def test_sigma_block_vs_oracle(L, N, seed, nv, kernel, synth, dg):
 def test_sigma_plan(synth, dg):
     """doci_sigma_plan reports the path doci_sigma takes: the automatic choice
     resolves to the mma.sync pair form for FP32 (a diag * x pass and the pair
-    pass) once the tiling gives every SM work, to a row pass for FP64 (or
-    the shape's tuned choice), the gather kernel on small spaces; an explicit
+    pass) and to the float-float pair form for FP64 (x conversion with the
+    diag * x pass, and the pair pass) once the tiling gives every SM work (or
+    to the shape's tuned choice), the gather kernel on small spaces; an explicit
     kind is honoured (the tensor-core pair form: one launch for the rows
     without column elements and one per row-part size of the (N-1)-pair sets,
     11 at L=20, N=10, split 9), FP32-only kinds take the automatic FP64 path,
@@ -252,7 +253,7 @@ def test_sigma_plan(synth, dg):
     with dg.Hamiltonian.from_fcidump(synth(20, 10, 51)) as h:
         assert h.sigma_plan(dg.FP32) == (6, 2)
         auto64 = h.sigma_plan(dg.FP64)
-        assert auto64[0] in (1, 3, 4)
+        assert auto64 in ((9, 2), (1, 1), (3, 1), (4, 1))  # the float-float pair form, or a tuned choice
         h.set_sigma_kernel("row1")
         assert h.sigma_plan(dg.FP32) == (3, 1)
         h.set_sigma_kernel("pair")
