@@ -44,7 +44,45 @@ int solve_roots(doci_ham *h, const doci_batch_opts &o, cudaStream_t st, doci_roo
   return engine_solve(1, &h, o, st, res, v);
 }
 
-int64_t roots_footprint(int L, int N, const doci_batch_opts &o) { return engine_footprint(L, N, o); }
+int64_t roots_footprint(int L, int N, const doci_batch_opts &o) {
+  const int64_t e = engine_footprint(L, N, o);
+  if (o.nroots != 1 || e < 0) return e;
+  doci_solve_opts so;
+  doci_solve_opts_default(&so);
+  so.mode = o.mode;
+  so.davidson_max_vec = o.max_vec;
+  const int64_t d = doci_solve_footprint(L, N, &so, 1);
+  return d > e ? d : e;
+}
+
+// A one-root request of the server: the single-root device Davidson
+// (doci_solve on the request's own handle and stream; mixed or FP64 as the
+// options say), which needs fewer vector passes per iteration than the
+// block engine.
+int solve_single(doci_ham *h, const doci_batch_opts &o, doci_root_result *res) {
+  doci_solve_opts so;
+  doci_solve_opts_default(&so);
+  so.solver = DOCI_SOLVER_D;
+  so.max_its = o.max_its;
+  so.tol = o.tol;
+  so.mode = o.mode;
+  so.mixed_tol = o.mixed_tol;
+  so.davidson_max_vec = o.max_vec;
+  so.davidson_keep = 2;
+  so.print_level = 0;
+  doci_solve_result r;
+  const int s = doci_solve(h, &so, nullptr, &r);
+  if (s != DOCI_OK) return s;
+  res->nroots = 1;
+  res->energy[0] = r.energy;
+  res->residual[0] = r.residual;
+  res->energy_fp32[0] = r.energy_fp32;
+  res->iterations = r.iterations;
+  res->iterations_fp32 = r.iterations_fp32;
+  res->sigmas = r.iterations;
+  res->converged = r.converged;
+  return DOCI_OK;
+}
 
 }  // namespace
 
@@ -143,7 +181,7 @@ struct doci_server {
       s = ham_build(h, in);
       own = true;
     }
-    if (s == DOCI_OK) s = solve_roots(h, opts, st, res, nullptr);
+    if (s == DOCI_OK) s = opts.nroots == 1 ? solve_single(h, opts, res) : solve_roots(h, opts, st, res, nullptr);
     if (own) {
       ham_release(h);
       delete h;

@@ -11,8 +11,9 @@
 //   -> thick restart where the basis is full (deflation pass)
 //   -> residuals and diagonal-preconditioned corrections of every root
 //   -> convergence / stall decisions (one thread per problem)
-//   -> classical Gram-Schmidt, twice, of each correction of an unconverged
-//      root against the basis (projection passes with FP64 sums)
+//   -> classical Gram-Schmidt of each correction of an unconverged root
+//      against the basis, a second pass when the first leaves less than half
+//      of its norm (projection passes with FP64 sums)
 //   -> sigma of the new basis vectors (one multi-problem, multi-vector pass)
 //   -> the new columns of the subspace matrices.
 //
@@ -72,7 +73,7 @@ struct EProb {
 };
 
 struct EState {
-  int m, m0, its, done, converged, stall, restart, kk, nact, added, sigmas, idx0;
+  int m, m0, its, done, converged, stall, restart, kk, nact, added, sigmas, idx0, need2;
   int act[kMaxR];
   double best, n0, n1, scale;
   double res[kMaxR];
@@ -293,12 +294,15 @@ __global__ void __launch_bounds__(kET) eng_residual(EArgs a, int q) {
     if (threadIdx.x == 0) st.res[q] = sqrt(out[0]);
 }
 
-// projections of correction act[q]: [t.t, V_k.t]; with `update` first
-// t -= sum_k c_k V_k (c from the previous projection)
+// projections of correction act[q]: [t.t, V_k.t]; with `update` (1: first
+// pass, 2: second pass) first t -= sum_k c_k V_k (c from the previous
+// projection).  The second pass runs only when the first left less than half
+// of the correction's norm (the Daniel-Gragg-Kaufman-Stewart test).
 template <typename S, int KM>
 __global__ void __launch_bounds__(kET) eng_gs(EArgs a, int q, int update) {
   ENG_CHUNK_PROLOGUE
   if (st.done || q >= st.nact) return;
+  if (update == 2 && !st.need2) return;
   const int m = st.m;
   __shared__ S cs[KM];
   if (threadIdx.x < KM) cs[threadIdx.x] = (update && threadIdx.x < m) ? static_cast<S>(st.c[threadIdx.x]) : S(0);
@@ -338,6 +342,7 @@ __global__ void __launch_bounds__(kET) eng_gs(EArgs a, int q, int update) {
         st.n0 = out[0];
       } else {
         st.n1 = out[0];
+        if (update == 1) st.need2 = !(out[0] > 0.25 * st.n0);
       }
     }
   }
@@ -721,7 +726,7 @@ int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool
     for (int q = 0; q < R; ++q) {
       eng_gs<S, KM><<<nblk(nchunks), kET, 0, st>>>(a, q, 0);
       eng_gs<S, KM><<<nblk(nchunks), kET, 0, st>>>(a, q, 1);
-      eng_gs<S, KM><<<nblk(nchunks), kET, 0, st>>>(a, q, 1);
+      eng_gs<S, KM><<<nblk(nchunks), kET, 0, st>>>(a, q, 2);
       eng_orth_decide<<<small, 128, 0, st>>>(a, q);
       eng_gs_finish<S><<<nblk(nchunks), kET, 0, st>>>(a, q);
       eng_orth_commit<<<small, 128, 0, st>>>(a, q, q == R - 1);

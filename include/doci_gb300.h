@@ -378,7 +378,10 @@ int doci_batch_solve(int n, doci_ham *const *hams, const doci_batch_opts *opts, 
 
 /* Request server: submitted requests (integrals or an FCIDUMP path) are
  * admitted as workers and memory free up, built on the device and solved
- * concurrently (continuous batching).  Tickets identify requests. */
+ * concurrently, each on its own stream (continuous batching): one-root
+ * requests by the single-root device Davidson (doci_solve's solver, mode and
+ * mixed_tol from opts), several roots by the batch engine.  Tickets identify
+ * requests. */
 typedef struct doci_server doci_server;
 int doci_server_create(const doci_batch_opts *opts, doci_server **out);
 int doci_server_submit(doci_server *srv, int L, int n_pairs, double core, const double *one, const double *two,

@@ -3,8 +3,9 @@
 Roots 2-4 have no reference counterpart (the reference is single-root): they
 are checked against a dense diagonalisation of the Hamiltonian built column
 by column from the oracle's matvec; the lowest root against the reference's
-golden energy.  Batched and served results must be bit-identical to the same
-solve run alone."""
+golden energy.  Batched results must be bit-identical to the same solve run
+alone; served one-root results equal the same single-root solve run alone to
+1e-9 Ha."""
 import numpy as np
 import pytest
 
@@ -78,7 +79,11 @@ def test_server_continuous_batching(dg):
     for L, N, seed in reqs:
         one, two = raw_integrals(L, seed)
         with dg.Hamiltonian.from_integrals(L, N, 0.0, one, two) as h:
-            alone[seed] = dg.solve_roots(h, nroots=1, tol=1e-6, mode="mixed")
+            # a one-root request runs the single-root device Davidson with the
+            # server's options (doci_batch_opts defaults: MAX_VEC 16, mixed_tol 1e-4)
+            r, _ = h.solve(solver="D", tol=1e-6, mode="mixed", mixed_tol=1e-4, davidson_max_vec=16,
+                           davidson_keep=2, max_its=200)
+            alone[seed] = r
     with dg.Server(nroots=1, tol=1e-6, mode="mixed", workers=5) as srv:
         tickets = {}
         for L, N, seed in reqs:
@@ -91,8 +96,9 @@ def test_server_continuous_batching(dg):
         assert s["submitted"] == s["finished"] == len(reqs) and s["bytes_in_use"] == 0
     overlapped = 0
     for seed, r in results.items():
-        assert r["status"] == 0
-        assert r["energies"] == alone[seed]["energies"]  # same alone and in the mix
+        assert r["status"] == 0 and r["converged"] == 1
+        # same alone and in the mix, within the rounding of the FP32 sigma's atomic adds
+        assert abs(r["energies"][0] - alone[seed]["energy"]) <= 1e-9
         assert r["queued_s"] <= r["start_s"] <= r["end_s"]
         overlapped += any(o is not r and o["start_s"] < r["end_s"] and r["start_s"] < o["end_s"]
                           for o in results.values())
