@@ -52,7 +52,7 @@ namespace doci {
 namespace {
 
 constexpr int kET = 256;                // threads per block of the batched passes
-constexpr int kEPer = 16;               // vector-pass elements per thread
+constexpr int kEPer = 32;               // vector-pass elements per thread (FP32 partial sums over them)
 constexpr int kEChunk = kET * kEPer;    // vector-pass chunk
 constexpr int kMaxR = 8;                // roots
 constexpr int kMaxV = 32;               // basis vectors
@@ -448,55 +448,88 @@ __global__ void __launch_bounds__(kET) eng_unit(EArgs a) {
 }
 
 // ---------------------------------------------------------------- per-problem control
-// the R smallest diagonal elements (one block per problem), stored in act[]
-__global__ void __launch_bounds__(1024) eng_lowest(EArgs a) {
-  const int p = blockIdx.x;
-  const EProb &pb = a.P[p];
-  EState &st = a.St[p];
-  __shared__ double bv[32];
-  __shared__ uint32_t bi[32];
-  __shared__ uint32_t picked[kMaxR];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// round r of the start-vector choice: the r-th smallest diagonal element
+// (the first index on ties, excluding the r already chosen), stored in
+// act[r]; every chunk finds its minimum, the problem's last chunk to arrive
+// takes the minimum over the chunks in chunk order
+__global__ void __launch_bounds__(kET) eng_lowest(EArgs a, int r) {
+  ENG_CHUNK_PROLOGUE
   const int R = a.R < static_cast<int>(pb.D) ? a.R : static_cast<int>(pb.D);
-  for (int r = 0; r < R; ++r) {
-    double v = 1e308;
-    uint32_t id = 0xffffffffu;
-    for (uint32_t j = threadIdx.x; j < pb.D; j += blockDim.x) {
-      bool taken = false;
-      for (int s = 0; s < r; ++s) taken |= picked[s] == j;
-      const double d = pb.diag[j];
-      if (!taken && (d < v || (d == v && j < id))) {
-        v = d;
-        id = j;
-      }
+  if (r >= R) return;
+  __shared__ double wv[kET / 32];
+  __shared__ uint32_t wi[kET / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double v = 1e308;
+  uint32_t id = 0xffffffffu;
+  for (int e = 0; e < kEPer; ++e) {
+    const uint32_t jj = jbase + e * kET;
+    if (jj >= pb.D) break;
+    bool taken = false;
+    for (int q = 0; q < r; ++q) taken |= static_cast<uint32_t>(st.act[q]) == jj;
+    const double d = pb.diag[jj];
+    if (!taken && (d < v || (d == v && jj < id))) {
+      v = d;
+      id = jj;
     }
+  }
+  auto better = [](double v2, uint32_t i2, double v1, uint32_t i1) { return v2 < v1 || (v2 == v1 && i2 < i1); };
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double v2 = __shfl_down_sync(0xffffffffu, v, o);
-      const uint32_t i2 = __shfl_down_sync(0xffffffffu, id, o);
-      if (v2 < v || (v2 == v && i2 < id)) {
-        v = v2;
-        id = i2;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_down_sync(0xffffffffu, v, o);
+    const uint32_t i2 = __shfl_down_sync(0xffffffffu, id, o);
+    if (better(v2, i2, v, id)) {
+      v = v2;
+      id = i2;
+    }
+  }
+  if (lane == 0) {
+    wv[warp] = v;
+    wi[warp] = id;
+  }
+  __syncthreads();
+  double *row = a.part + static_cast<size_t>(pb.chunk0 + chunk) * kLdp;
+  if (threadIdx.x == 0) {
+    double bv = wv[0];
+    uint32_t bi = wi[0];
+    for (int w = 1; w < kET / 32; ++w)
+      if (better(wv[w], wi[w], bv, bi)) {
+        bv = wv[w];
+        bi = wi[w];
       }
+    row[0] = bv;
+    row[1] = static_cast<double>(bi);
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(a.cnt + p, 1u) == pb.nchunks - 1;
+  __syncthreads();
+  if (!last || warp != 0) return;
+  __threadfence();
+  const double *r0 = a.part + static_cast<size_t>(pb.chunk0) * kLdp;
+  v = 1e308;
+  id = 0xffffffffu;
+  for (uint32_t c = lane; c < pb.nchunks; c += 32) {
+    const double v2 = __ldcg(r0 + static_cast<size_t>(c) * kLdp);
+    const uint32_t i2 = static_cast<uint32_t>(__ldcg(r0 + static_cast<size_t>(c) * kLdp + 1));
+    if (better(v2, i2, v, id)) {
+      v = v2;
+      id = i2;
     }
-    if (lane == 0) {
-      bv[warp] = v;
-      bi[warp] = id;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_down_sync(0xffffffffu, v, o);
+    const uint32_t i2 = __shfl_down_sync(0xffffffffu, id, o);
+    if (better(v2, i2, v, id)) {
+      v = v2;
+      id = i2;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double bvv = bv[0];
-      uint32_t bii = bi[0];
-      for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w)
-        if (bv[w] < bvv || (bv[w] == bvv && bi[w] < bii)) {
-          bvv = bv[w];
-          bii = bi[w];
-        }
-      picked[r] = bii;
-      st.act[r] = static_cast<int>(bii);
-      if (r == 0) st.idx0 = static_cast<int>(bii);
-    }
-    __syncthreads();
+  }
+  if (lane == 0) {
+    st.act[r] = static_cast<int>(id);
+    if (r == 0) st.idx0 = static_cast<int>(id);
+    a.cnt[p] = 0;
   }
 }
 
@@ -518,24 +551,30 @@ __global__ void eng_init_state(EArgs a) {
   a.flags[p] = 1;
 }
 
-// the subspace eigenproblem of every running problem: one warp, cyclic
-// Jacobi in FP64 (lanes over the rows of the rotated columns), ascending
-// eigenvalues; then the restart decision
+// the subspace eigenproblem of every running problem: one warp, Jacobi in
+// FP64 with the round-robin (tournament) ordering: each round rotates n/2
+// disjoint index pairs at once (one lane computes each rotation, lanes then
+// apply them over rows and columns), n-1 rounds a sweep, until the
+// off-diagonal part is below 1e-30 of the whole; ascending eigenvalues; then
+// the restart decision
 __global__ void __launch_bounds__(32) eng_eig(EArgs a) {
   const int p = blockIdx.x;
   EState &st = a.St[p];
   if (st.done) return;
   __shared__ double A[kMaxV * kMaxV], Vv[kMaxV * kMaxV];
+  __shared__ double rc[kMaxV / 2], rs[kMaxV / 2];
+  __shared__ int rp[kMaxV / 2], rq[kMaxV / 2];
   __shared__ double wv[kMaxV];
   __shared__ int idx[kMaxV];
   const int n = st.m, lane = threadIdx.x;
+  const int n2 = n + (n & 1), half = n2 / 2;
   for (int i = lane; i < kMaxV * kMaxV; i += 32) {
     const int r = i % kMaxV, c = i / kMaxV;
     A[i] = (r < n && c < n) ? st.S[i] : 0.0;
     Vv[i] = (r == c) ? 1.0 : 0.0;
   }
   __syncwarp();
-  for (int sweep = 0; sweep < 100; ++sweep) {
+  for (int sweep = 0; sweep < 100 && n > 1; ++sweep) {
     double off = 0, tot = 0;
     for (int i = lane; i < n * n; i += 32) {
       const int r = i % n, c = i / n;
@@ -549,30 +588,57 @@ __global__ void __launch_bounds__(32) eng_eig(EArgs a) {
       tot += __shfl_xor_sync(0xffffffffu, tot, o);
     }
     if (off == 0 || off <= 1e-30 * tot) break;
-    for (int pp = 0; pp < n - 1; ++pp)
-      for (int qq = pp + 1; qq < n; ++qq) {
-        const double apq = A[qq * kMaxV + pp];
-        if (apq == 0) continue;
-        const double theta = (A[qq * kMaxV + qq] - A[pp * kMaxV + pp]) / (2 * apq);
-        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
-        const double cs = 1 / sqrt(t * t + 1), sn = t * cs;
-        __syncwarp();
-        if (lane < n) {  // columns p, q
+    for (int round = 0; round < n2 - 1; ++round) {
+      if (lane < half) {
+        auto player = [&](int k) { return k == 0 ? 0 : ((k - 1 + round) % (n2 - 1)) + 1; };
+        int pp = player(lane), qq = player(n2 - 1 - lane);
+        if (pp > qq) {
+          const int t = pp;
+          pp = qq;
+          qq = t;
+        }
+        double cs = 1.0, sn = 0.0;
+        if (qq < n) {
+          const double apq = A[qq * kMaxV + pp];
+          if (apq != 0) {
+            const double theta = (A[qq * kMaxV + qq] - A[pp * kMaxV + pp]) / (2 * apq);
+            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
+            cs = 1 / sqrt(t * t + 1);
+            sn = t * cs;
+          }
+        }
+        rp[lane] = pp;
+        rq[lane] = qq;
+        rc[lane] = cs;
+        rs[lane] = sn;
+      }
+      __syncwarp();
+      if (lane < n) {
+        for (int i = 0; i < half; ++i) {  // columns p, q of row `lane`
+          const int pp = rp[i], qq = rq[i];
+          if (qq >= n || rs[i] == 0.0) continue;
+          const double cs = rc[i], sn = rs[i];
           const double akp = A[pp * kMaxV + lane], akq = A[qq * kMaxV + lane];
           A[pp * kMaxV + lane] = cs * akp - sn * akq;
           A[qq * kMaxV + lane] = sn * akp + cs * akq;
-        }
-        __syncwarp();
-        if (lane < n) {  // rows p, q
-          const double apk = A[lane * kMaxV + pp], aqk = A[lane * kMaxV + qq];
-          A[lane * kMaxV + pp] = cs * apk - sn * aqk;
-          A[lane * kMaxV + qq] = sn * apk + cs * aqk;
           const double vkp = Vv[pp * kMaxV + lane], vkq = Vv[qq * kMaxV + lane];
           Vv[pp * kMaxV + lane] = cs * vkp - sn * vkq;
           Vv[qq * kMaxV + lane] = sn * vkp + cs * vkq;
         }
-        __syncwarp();
       }
+      __syncwarp();
+      if (lane < n) {
+        for (int i = 0; i < half; ++i) {  // rows p, q of column `lane`
+          const int pp = rp[i], qq = rq[i];
+          if (qq >= n || rs[i] == 0.0) continue;
+          const double cs = rc[i], sn = rs[i];
+          const double apk = A[lane * kMaxV + pp], aqk = A[lane * kMaxV + qq];
+          A[lane * kMaxV + pp] = cs * apk - sn * aqk;
+          A[lane * kMaxV + qq] = sn * apk + cs * aqk;
+        }
+      }
+      __syncwarp();
+    }
   }
   __syncwarp();
   if (lane == 0) {
@@ -715,7 +781,7 @@ int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool
   const unsigned small = (n + 127) / 128;
   eng_init_state<<<small, 128, 0, st>>>(a);
   if (unit_start) {
-    eng_lowest<<<n, 1024, 0, st>>>(a);
+    for (int r = 0; r < R; ++r) eng_lowest<<<nblk(nchunks), kET, 0, st>>>(a, r);
     eng_unit<S><<<nblk(nchunks), kET, 0, st>>>(a);
     eng_init_state<<<small, 128, 0, st>>>(a);
   }
@@ -1064,7 +1130,7 @@ int engine_solve(int n, doci_ham *const *hams, const doci_batch_opts &o, cudaStr
       }
       if ((s = upload())) return s;
       eng_init_state<<<(n + 127) / 128, 128, 0, st>>>(a);
-      eng_lowest<<<n, 1024, 0, st>>>(a);
+      eng_lowest<<<nblk(nchunks), kET, 0, st>>>(a, 0);
       DOCI_CUDA(cudaGetLastError());
       DOCI_CUDA(cudaMemcpyAsync(host_st.data(), dS.p, sizeof(EState) * n, cudaMemcpyDeviceToHost, st));
       DOCI_CUDA(cudaStreamSynchronize(st));
