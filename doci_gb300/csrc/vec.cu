@@ -243,6 +243,12 @@ constexpr int kChunk = 16;
 // accumulators: 37 / 35 KB of static shared memory).
 template <int K>
 __host__ __device__ constexpr int f32_block() { return K <= 16 ? 256 : 128; }
+// resident blocks per SM the register budget is set for (three, so at most
+// 85 registers for 256-thread blocks), launched as one full wave.  Measured on
+// GB300 (residual pass, 16 vectors, L=32 size): 87 registers and two resident
+// blocks per SM 58.5 ms, 80 registers and three 15.9 ms.
+template <int K>
+__host__ __device__ constexpr int f32_minb() { return 3; }
 
 template <int NK, int BT>
 struct SmemAcc {
@@ -265,7 +271,7 @@ struct SmemAcc {
 };
 
 template <int K>
-__global__ void __launch_bounds__(f32_block<K>())
+__global__ void __launch_bounds__(f32_block<K>(), f32_minb<K>())
 multidot_f32_kernel(const float *__restrict__ V, size_t ld, int m, const float *__restrict__ w, size_t n,
                     double *__restrict__ partials) {
   __shared__ double acc_s[K * f32_block<K>()];
@@ -291,7 +297,7 @@ multidot_f32_kernel(const float *__restrict__ V, size_t ld, int m, const float *
 }
 
 template <int K>
-__global__ void __launch_bounds__(f32_block<K>())
+__global__ void __launch_bounds__(f32_block<K>(), f32_minb<K>())
 residual_f32_kernel(const float *__restrict__ V, const float *__restrict__ VA, size_t ld, int m,
                     const double *__restrict__ y, double theta, double pre_theta, const double *__restrict__ diag,
                     size_t n, float *__restrict__ t, double *__restrict__ x_out, double *__restrict__ partials) {
@@ -336,7 +342,7 @@ residual_f32_kernel(const float *__restrict__ V, const float *__restrict__ VA, s
 }
 
 template <int K>
-__global__ void __launch_bounds__(f32_block<K>())
+__global__ void __launch_bounds__(f32_block<K>(), f32_minb<K>())
 gs_update_f32_kernel(const float *__restrict__ V, size_t ld, int m, const double *__restrict__ c, size_t n,
                      float *__restrict__ t, double *__restrict__ partials) {
   __shared__ float cs[K];
@@ -449,7 +455,7 @@ combine_f32_kernel(const float *__restrict__ V, size_t ld, int m, const double *
 // coefficient, like the FP32 rounding of its sigma.
 
 template <int K>
-__global__ void __launch_bounds__(f32_block<K>())
+__global__ void __launch_bounds__(f32_block<K>(), f32_minb<K>())
 multidot_mix_kernel(const double *__restrict__ V, size_t ld, int m, const double *__restrict__ w, size_t n,
                     double *__restrict__ partials) {
   __shared__ double acc_s[K * f32_block<K>()];
@@ -478,7 +484,7 @@ multidot_mix_kernel(const double *__restrict__ V, size_t ld, int m, const double
 }
 
 template <int K>
-__global__ void __launch_bounds__(f32_block<K>())
+__global__ void __launch_bounds__(f32_block<K>(), f32_minb<K>())
 residual_mix_kernel(const double *__restrict__ V, const double *__restrict__ VA, size_t ld, int m,
                     const double *__restrict__ y, double theta, double pre_theta, const double *__restrict__ diag,
                     size_t n, double *__restrict__ t, double *__restrict__ x_out, double *__restrict__ partials) {
@@ -532,7 +538,7 @@ residual_mix_kernel(const double *__restrict__ V, const double *__restrict__ VA,
 }
 
 template <int K>
-__global__ void __launch_bounds__(f32_block<K>())
+__global__ void __launch_bounds__(f32_block<K>(), f32_minb<K>())
 gs_update_mix_kernel(const double *__restrict__ V, size_t ld, int m, const double *__restrict__ c, size_t n,
                      double *__restrict__ t, double *__restrict__ partials) {
   __shared__ float cs[K];
@@ -739,10 +745,8 @@ __global__ void fill_random_kernel(double *__restrict__ t, size_t n, uint64_t se
 // FP32-storage update passes (Gram-Schmidt finish, deflation, combination):
 // one full wave (SMs x resident blocks of the kernel, at most 2
 // grid_blocks()), so no partial last wave idles most SMs (measured: the
-// finish pass at 16 vectors, L=32, 14.4 -> 10.7 ms); the projection passes
-// measured faster with grid_blocks() x 256 threads in flight.  The FP64
-// passes keep grid_blocks() (their summation order, hence the FP64 results,
-// stay fixed).
+// finish pass at 16 vectors, L=32, 14.4 -> 10.7 ms).  The FP64 passes keep
+// grid_blocks() (their summation order, hence the FP64 results, stay fixed).
 template <typename KernelT>
 int wave_grid(KernelT kern, int threads) {
   static std::atomic<int> per_sm{0};  // one value per kernel instantiation (the query is a driver call)
@@ -769,7 +773,7 @@ template <typename S, int K>
 struct MultidotL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const S *w, size_t n, double *p) {
     if constexpr (std::is_same<S, float>::value)
-      multidot_f32_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, ld, m, w, n, p);
+      multidot_f32_kernel<K><<<wave_grid(multidot_f32_kernel<K>, f32_block<K>()), f32_block<K>(), 0, st>>>(V, ld, m, w, n, p);
     else
       multidot_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, w, n, p);
   }
@@ -778,7 +782,7 @@ template <typename S, int K>
 struct MultidotMixL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const S *w, size_t n, double *p) {
     if constexpr (std::is_same<S, double>::value)
-      multidot_mix_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, ld, m, w, n, p);
+      multidot_mix_kernel<K><<<wave_grid(multidot_mix_kernel<K>, f32_block<K>()), f32_block<K>(), 0, st>>>(V, ld, m, w, n, p);
   }
 };
 template <typename S, int K>
@@ -786,7 +790,7 @@ struct ResidualMixL {
   static void run(int g, cudaStream_t st, const S *V, const S *VA, size_t ld, int m, const double *y, double th,
                   double pre, const double *diag, size_t n, S *t, double *x, double *p) {
     if constexpr (std::is_same<S, double>::value)
-      residual_mix_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, VA, ld, m, y, th, pre, diag, n,
+      residual_mix_kernel<K><<<wave_grid(residual_mix_kernel<K>, f32_block<K>()), f32_block<K>(), 0, st>>>(V, VA, ld, m, y, th, pre, diag, n,
                                                                               t, x, p);
   }
 };
@@ -794,7 +798,7 @@ template <typename S, int K>
 struct GsUpdateMixL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *p) {
     if constexpr (std::is_same<S, double>::value)
-      gs_update_mix_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, ld, m, c, n, t, p);
+      gs_update_mix_kernel<K><<<wave_grid(gs_update_mix_kernel<K>, f32_block<K>()), f32_block<K>(), 0, st>>>(V, ld, m, c, n, t, p);
   }
 };
 template <typename S, int K>
@@ -816,7 +820,7 @@ struct ResidualL {
   static void run(int g, cudaStream_t st, const S *V, const S *VA, size_t ld, int m, const double *y, double th,
                   double pre, const double *diag, size_t n, S *t, double *x, double *p) {
     if constexpr (std::is_same<S, float>::value)
-      residual_f32_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, VA, ld, m, y, th, pre, diag, n,
+      residual_f32_kernel<K><<<wave_grid(residual_f32_kernel<K>, f32_block<K>()), f32_block<K>(), 0, st>>>(V, VA, ld, m, y, th, pre, diag, n,
                                                                               t, x, p);
     else
       residual_kernel<S, K><<<g, kT, 0, st>>>(V, VA, ld, m, y, th, pre, diag, n, t, x, p);
@@ -826,7 +830,7 @@ template <typename S, int K>
 struct GsUpdateL {
   static void run(int g, cudaStream_t st, const S *V, size_t ld, int m, const double *c, size_t n, S *t, double *p) {
     if constexpr (std::is_same<S, float>::value)
-      gs_update_f32_kernel<K><<<g * kT / f32_block<K>(), f32_block<K>(), 0, st>>>(V, ld, m, c, n, t, p);
+      gs_update_f32_kernel<K><<<wave_grid(gs_update_f32_kernel<K>, f32_block<K>()), f32_block<K>(), 0, st>>>(V, ld, m, c, n, t, p);
     else
       gs_update_kernel<S, K><<<g, kT, 0, st>>>(V, ld, m, c, n, t, p);
   }
