@@ -214,6 +214,12 @@ __global__ void __launch_bounds__(kET) eng_sigma(EArgs a) {
 }
 
 // ---------------------------------------------------------------- vector passes
+// three resident blocks per SM for the FP32 phase's passes (register
+// budget 85; at two per SM the projection passes ran at ~2.4 TB/s); the
+// FP64 phase's few iterations keep the registers their arrays need
+template <typename S>
+constexpr int eng_minb() { return sizeof(S) == 4 ? 3 : 1; }
+
 // chunk-local element range of this thread: j = base + e * kET, e < kEPer
 #define ENG_CHUNK_PROLOGUE                                      \
   const int p = owner(a.chunk0, a.n, blockIdx.x);               \
@@ -224,7 +230,7 @@ __global__ void __launch_bounds__(kET) eng_sigma(EArgs a) {
 
 // products summed over the thread's elements in S, then into FP64
 template <typename S, int KM>
-__global__ void __launch_bounds__(kET) eng_subcol(EArgs a, int j) {
+__global__ void __launch_bounds__(kET, eng_minb<S>()) eng_subcol(EArgs a, int j) {
   ENG_CHUNK_PROLOGUE
   if (st.done) return;
   const int i = st.m0 + j;
@@ -299,7 +305,7 @@ __global__ void __launch_bounds__(kET) eng_residual(EArgs a, int q) {
 // projection).  The second pass runs only when the first left less than half
 // of the correction's norm (the Daniel-Gragg-Kaufman-Stewart test).
 template <typename S, int KM>
-__global__ void __launch_bounds__(kET) eng_gs(EArgs a, int q, int update) {
+__global__ void __launch_bounds__(kET, eng_minb<S>()) eng_gs(EArgs a, int q, int update) {
   ENG_CHUNK_PROLOGUE
   if (st.done || q >= st.nact) return;
   if (update == 2 && !st.need2) return;
