@@ -898,10 +898,17 @@ __global__ void copy4_kernel(const uint32_t *__restrict__ src, uint32_t *__restr
 
 int vec_copy(void *dst, const void *src, size_t bytes, cudaStream_t st) {
   const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src);
-  if ((a % 16) == 0 && (bytes % 16) == 0)
-    copy16_kernel<<<grid_blocks() * 2, kT, 0, st>>>(static_cast<const uint4 *>(src), static_cast<uint4 *>(dst),
-                                                    bytes / 16);
-  else if ((a % 4) == 0 && (bytes % 4) == 0)
+  if ((a % 16) == 0 && (bytes % 4) == 0) {
+    // 16-byte words for the bulk (D x 4 bytes is rarely a multiple of 16:
+    // copying all of it in 4-byte words over the host link is much slower),
+    // then the last one to three words
+    const size_t n16 = bytes / 16, tail = bytes - n16 * 16;
+    if (n16)
+      copy16_kernel<<<grid_blocks() * 2, kT, 0, st>>>(static_cast<const uint4 *>(src), static_cast<uint4 *>(dst), n16);
+    if (tail)
+      copy4_kernel<<<1, 32, 0, st>>>(reinterpret_cast<const uint32_t *>(static_cast<const char *>(src) + n16 * 16),
+                                     reinterpret_cast<uint32_t *>(static_cast<char *>(dst) + n16 * 16), tail / 4);
+  } else if ((a % 4) == 0 && (bytes % 4) == 0)
     copy4_kernel<<<grid_blocks() * 2, kT, 0, st>>>(static_cast<const uint32_t *>(src), static_cast<uint32_t *>(dst),
                                                    bytes / 4);
   else
