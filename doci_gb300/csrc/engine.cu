@@ -27,7 +27,9 @@
 // bit-identical alone and in any batch.  Large problems (from 2^22
 // determinants, or as the shape's autotuning decides) take their sigmas from
 // the single-problem kernels (launch_sigma: the pair form for FP32) on
-// staging buffers instead; their results still do not depend on the batch,
+// staging buffers instead (each on one of up to eight streams forked from
+// and joined back into the engine's stream, so that several problems'
+// kernels overlap); their results still do not depend on the batch,
 // but the FP32 pair form's atomic adds make their last bits vary from run to
 // run.  Mixed mode: an FP32 phase on H - s (s = the lowest diagonal
 // element; FP32 basis, sigma and vector arithmetic with FP64 sums), ending at
@@ -769,6 +771,44 @@ struct DBuf {
 
 inline unsigned nblk(uint64_t n) { return static_cast<unsigned>(n < 1 ? 1 : n); }
 
+constexpr size_t kSideStreams = 8;
+
+// streams forked from the engine's stream and joined back into it
+struct SideStreams {
+  int n = 0;
+  cudaStream_t s[kSideStreams] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kSideStreams] = {};
+  int make(int count) {
+    DOCI_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    for (int i = 0; i < count; ++i) {
+      DOCI_CUDA(cudaStreamCreateWithFlags(&s[i], cudaStreamNonBlocking));
+      DOCI_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
+      n = i + 1;
+    }
+    return DOCI_OK;
+  }
+  cudaError_t fork(cudaStream_t st) {
+    cudaError_t e = cudaEventRecord(fork_ev, st);
+    for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(s[i], fork_ev, 0);
+    return e;
+  }
+  cudaError_t join(cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < n && e == cudaSuccess; ++i) {
+      e = cudaEventRecord(join_ev[i], s[i]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, join_ev[i], 0);
+    }
+    return e;
+  }
+  ~SideStreams() {
+    for (int i = 0; i < n; ++i) {
+      cudaStreamDestroy(s[i]);
+      cudaEventDestroy(join_ev[i]);
+    }
+    if (fork_ev) cudaEventDestroy(fork_ev);
+  }
+};
+
 // a problem whose sigmas come from launch_sigma (its handle, or the FP32
 // phase's shifted view of it) through staging buffers of R vectors
 struct BigProb {
@@ -785,6 +825,14 @@ int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool
   const int prec = sizeof(S) == 8 ? DOCI_FP64 : DOCI_FP32;
   std::vector<char> big_running(big.size(), 1);
   const unsigned small = (n + 127) / 128;
+  // side streams for the large problems' sigmas: each problem's copies and
+  // kernels run on one of them, so that several problems' kernels overlap
+  // (forked from and joined back into st with events, also inside the graph)
+  SideStreams side;
+  if (big.size() > 1) {
+    const int ns = static_cast<int>(std::min<size_t>(big.size(), kSideStreams));
+    if (const int se = side.make(ns)) return se;
+  }
   eng_init_state<<<small, 128, 0, st>>>(a);
   if (unit_start) {
     for (int r = 0; r < R; ++r) eng_lowest<<<nblk(nchunks), kET, 0, st>>>(a, r);
@@ -804,19 +852,22 @@ int run_phase(EArgs &a, uint32_t ntiles, uint32_t nchunks, cudaStream_t st, bool
       eng_orth_commit<<<small, 128, 0, st>>>(a, q, q == R - 1);
     }
     if (ntiles > 0) eng_sigma<S, NH><<<nblk(ntiles), kET, 0, st>>>(a);
-    for (size_t b = 0; b < big.size(); ++b) {
+    if (side.n > 0) DOCI_CUDA(side.fork(st));
+    for (size_t b = 0, k = 0; b < big.size(); ++b) {
       if (!big_running[b]) continue;
       const BigProb &bp = big[b];
-      eng_stage<S><<<nblk(std::min<uint64_t>((bp.D * R + 255) / 256, 4096)), 256, 0, st>>>(
+      cudaStream_t sb = side.n > 0 ? side.s[k++ % side.n] : st;
+      eng_stage<S><<<nblk(std::min<uint64_t>((bp.D * R + 255) / 256, 4096)), 256, 0, sb>>>(
           a, bp.p, static_cast<S *>(bp.xs), nullptr, 0);
       for (int v = 0; v < R; ++v) {
         const int sv = launch_sigma(bp.h, static_cast<S *>(bp.xs) + v * bp.D, static_cast<S *>(bp.ys) + v * bp.D,
-                                    prec, st);
+                                    prec, sb);
         if (sv) return sv;
       }
-      eng_stage<S><<<nblk(std::min<uint64_t>((bp.D * R + 255) / 256, 4096)), 256, 0, st>>>(
+      eng_stage<S><<<nblk(std::min<uint64_t>((bp.D * R + 255) / 256, 4096)), 256, 0, sb>>>(
           a, bp.p, nullptr, static_cast<const S *>(bp.ys), 1);
     }
+    if (side.n > 0) DOCI_CUDA(side.join(st));
     for (int j = 0; j < R; ++j) eng_subcol<S, KM><<<nblk(nchunks), kET, 0, st>>>(a, j);
     DOCI_CUDA(cudaGetLastError());
     return DOCI_OK;
