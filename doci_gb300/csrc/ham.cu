@@ -69,7 +69,7 @@ void ham_release(doci_ham *h) {
   if (!h) return;
   cudaStream_t st = h->stream;
   void *bufs[] = {h->d_binom, h->d_Kmir64, h->d_Kmir32, h->d_tab64, h->d_diag, h->d_diag32, h->d_stage_x,
-                  h->d_stage_y, h->d_rows, h->d_rowstart, h->d_pblocks, h->d_kfrag, h->d_tc_err};  // d_rem/d_ins/d_tab_off are shared (per-process cache)
+                  h->d_stage_y, h->d_rows, h->d_rowstart, h->d_pblocks, h->d_kfrag, h->d_tc_err};  // d_rem/d_ins/d_ins_t/d_tab_off are shared (per-process cache)
   for (void *p : bufs) release_async(p, st);
   if (h->h_diag) cudaFreeHost(h->h_diag);
   if (st) {
@@ -85,7 +85,7 @@ void ham_release(doci_ham *h) {
   h->d_kfrag = nullptr;
   h->d_tc_err = nullptr;
   h->npblocks = 0;
-  h->d_rem = h->d_ins = h->d_tab_off = nullptr;
+  h->d_rem = h->d_ins = h->d_ins_t = h->d_tab_off = nullptr;
   h->h_diag = nullptr;
   h->stream = nullptr;
 }
@@ -251,7 +251,7 @@ int ham_build_rows(doci_ham *h) {
   {
     // cross-hop tables depend only on (device, split): built once per process
     static std::mutex mu;
-    static std::map<std::pair<int, int>, std::array<uint32_t *, 3>> cache;
+    static std::map<std::pair<int, int>, std::array<uint32_t *, 4>> cache;
     std::lock_guard<std::mutex> lk(mu);
     auto key = std::make_pair(h->device, split);
     auto it = cache.find(key);
@@ -259,18 +259,27 @@ int ham_build_rows(doci_ham *h) {
       std::vector<uint32_t> B(kBinomRows * kBinomCols), rem, ins, toff;
       fill_binom_table(B.data());
       dev::build_cross_tables(split, B.data(), kBinomCols, rem, ins, toff);
-      std::array<uint32_t *, 3> t{};
+      std::vector<uint32_t> ins_t(ins.size());
+      for (int j = 0; j <= split; ++j) {
+        const uint32_t n = B[split * kBinomCols + j];
+        for (uint32_t c = 0; c < n; ++c)
+          for (uint32_t e = 0; e < 16; ++e) ins_t[toff[j] + ((e >> 2) * n + c) * 4 + (e & 3)] = ins[toff[j] + 16 * c + e];
+      }
+      std::array<uint32_t *, 4> t{};
       DOCI_CUDA(cudaMalloc(&t[0], rem.size() * sizeof(uint32_t)));
       DOCI_CUDA(cudaMalloc(&t[1], ins.size() * sizeof(uint32_t)));
       DOCI_CUDA(cudaMalloc(&t[2], toff.size() * sizeof(uint32_t)));
+      DOCI_CUDA(cudaMalloc(&t[3], ins_t.size() * sizeof(uint32_t)));
       DOCI_CUDA(cudaMemcpy(t[0], rem.data(), rem.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
       DOCI_CUDA(cudaMemcpy(t[1], ins.data(), ins.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
       DOCI_CUDA(cudaMemcpy(t[2], toff.data(), toff.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+      DOCI_CUDA(cudaMemcpy(t[3], ins_t.data(), ins_t.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
       it = cache.emplace(key, t).first;
     }
     h->d_rem = it->second[0];
     h->d_ins = it->second[1];
     h->d_tab_off = it->second[2];
+    h->d_ins_t = it->second[3];
   }
   DOCI_CUDA(cudaStreamSynchronize(h->stream));
   return ham_build_pairs(h, start);

@@ -90,6 +90,10 @@ struct doci_ham {
   // cross-hop index tables of the phase-ordered row pass (addressing.cuh,
   // build_cross_tables)
   uint32_t *d_rem = nullptr, *d_ins = nullptr, *d_tab_off = nullptr;
+  // the insertion table in quads (entries 4q..4q+3 of column position c of
+  // size j at tab_off[j] + 4 (q C(split, j) + c)): a warp's 16-byte loads of
+  // one quad are consecutive (the pair kernels)
+  uint32_t *d_ins_t = nullptr;
   // pair form (sigma_pair.cu): one block per (N-1)-pair set's row part R',
   // {own row start or ~0, mask | k' << 24}, largest first; the K matrix split
   // into TF32 high and low parts (2 x 32 x 32 floats, mirrored orbitals; also

@@ -1,7 +1,8 @@
 // sigma_pair.cu -- FP32 sigma in the (N-1)-pair intermediate form on the
-// warp-level mma.sync path (kind 6).  The tensor-core version of the same form,
-// sigma_tc.cu (kind 8), is the automatic FP32 choice on sm_103a; this one
-// stays for x buffers that are not 16-byte aligned and for comparison.
+// warp-level mma.sync path (kind 6, the automatic FP32 choice once the
+// tiling gives every SM a unit), and the FP64-accurate float-float version
+// of the same form (kind 9).  The tcgen05 version of the FP32 form is
+// sigma_tc.cu (kind 8).
 //
 // Every off-diagonal element of the DOCI Hamiltonian is a pair hop
 // T -> T \ i u a with weight K_ia = (ia|ia) (doci.c:216-222).  Writing
@@ -85,13 +86,13 @@ __global__ void pair_init_kernel(uint32_t D, const float *__restrict__ diag, con
 // followed by the row-part holes of R' (the row-part elements of R' are in
 // every S, so their X entries are zero).  Own-row sums by global atomics, one
 // m-tile of the product at a time and the insertion entries re-read for the
-// scatter, so that four blocks fit an SM (registers <= 64): 32 warps per SM
-// hide the gathers' latency (37.1 ms at L=32, N=16, against 55.0 ms with the
-// own row's sums in shared memory and two blocks per SM).
+// scatter (four 16-byte loads per set, quad-interleaved so that a warp's
+// load covers 512 consecutive bytes), so that four blocks fit an SM
+// (registers <= 64): 32 warps per SM hide the gathers' latency.
 __global__ void __launch_bounds__(kPairThreads, 4)
 sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t *__restrict__ rowstart_of,
                   const uint32_t *__restrict__ g_binom, const float *__restrict__ g_ksplit,
-                  const uint32_t *__restrict__ ins, const uint32_t *__restrict__ ins_off,
+                  const uint32_t *__restrict__ ins_t, const uint32_t *__restrict__ ins_off,
                   const float *__restrict__ x, float *__restrict__ y) {
   __shared__ __align__(16) PairSmem sm;
   const uint32_t *B = g_binom;
@@ -134,7 +135,7 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
                                v1 ? __float_as_uint(__ldg(klo + o1 * 32 + oi)) : 0u);
     }
     __syncthreads();
-    const uint32_t *ins_blk = ins + ins_off[jp];
+    const uint32_t *ins_blk = ins_t + ins_off[jp];
 
     for (uint32_t s0 = 0; s0 < n_s; s0 += kPairThreads) {
       if (s0 + 32u * warp >= n_s) break;  // this warp's sets are all past the block (warp-uniform)
@@ -153,10 +154,10 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
       // table) and the row-part holes of R' (rows R' u b, column c)
       uint4 ent[4];
       if (live) {
-        const uint4 *ip = reinterpret_cast<const uint4 *>(ins_blk + 16u * c);
+        const uint4 *ip = reinterpret_cast<const uint4 *>(ins_blk);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (4 * u < nch) ent[u] = __ldg(ip + u);
+          if (4 * u < nch) ent[u] = __ldg(ip + (c + u * n_s));
 #pragma unroll
         for (int h = 0; h < 16; ++h)
           if (h < nch) {
@@ -215,10 +216,10 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
       // scatter Y_S back to the same determinants
       if (live) {
         {
-          const uint4 *ip = reinterpret_cast<const uint4 *>(ins_blk + 16u * c);
+          const uint4 *ip = reinterpret_cast<const uint4 *>(ins_blk);
 #pragma unroll
           for (int u = 0; u < 4; ++u)
-            if (4 * u < nch) ent[u] = __ldg(ip + u);
+            if (4 * u < nch) ent[u] = __ldg(ip + (c + u * n_s));
         }
 #pragma unroll
         for (int h = 0; h < 16; ++h)
@@ -247,7 +248,7 @@ template <int NO>
 __global__ void __launch_bounds__(kPairThreads, 2)
 sigma_pair_ff_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t *__restrict__ rowstart_of,
                      const uint32_t *__restrict__ g_binom, const double *__restrict__ g_K,
-                     const uint32_t *__restrict__ ins, const uint32_t *__restrict__ ins_off, const ff *__restrict__ x,
+                     const uint32_t *__restrict__ ins_t, const uint32_t *__restrict__ ins_off, const ff *__restrict__ x,
                      double *__restrict__ y) {
   __shared__ ff Kc[32 * 32];  // K on the block's slots: [output slot][input slot]
   __shared__ uint32_t hole_rs[32];
@@ -278,16 +279,15 @@ sigma_pair_ff_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32
     }
     __syncthreads();
     const uint32_t n_s = __ldg(B + sp * kBinomCols + jp);
-    const uint32_t *ins_blk = ins + ins_off[jp];
+    const uint32_t *ins_blk = ins_t + ins_off[jp];
     for (uint32_t c = threadIdx.x; c < n_s; c += blockDim.x) {
       ff X[NO];
       uint32_t tgt[NO];
       int slot[NO];
-      const uint32_t *ip = ins_blk + 16u * c;
 #pragma unroll
       for (int t = 0; t < NO; ++t) {
         if (t < nch) {
-          const uint32_t e = __ldg(ip + t);
+          const uint32_t e = __ldg(ins_blk + 4 * ((t >> 2) * n_s + c) + (t & 3));
           slot[t] = static_cast<int>(e & 0xffu);
           tgt[t] = own + (e >> 8);
         } else if (t < nopen) {
@@ -337,7 +337,7 @@ float round_tf32(double v) {
 
 bool pair_fits(const doci_ham *h) {
   if (h->split < 1 || h->split > 16 || h->nrows < 1 || !h->d_pblocks || h->npblocks < 1) return false;
-  if (!h->d_ins || !h->d_tab_off) return false;
+  if (!h->d_ins || !h->d_ins_t || !h->d_tab_off) return false;
   if (h->L - h->split > 24) return false;
   return static_cast<size_t>(h->max_row) * sizeof(float) <= 100 * 1024;
 }
@@ -398,7 +398,7 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
   int grid = sms * per_sm;
   if (grid > h->npblocks) grid = h->npblocks;
   sigma_pair_kernel<<<grid, kPairThreads, 0, st>>>(s, reinterpret_cast<const uint2 *>(h->d_pblocks), h->d_rowstart,
-                                                   h->d_binom, reinterpret_cast<const float *>(h->d_kfrag), h->d_ins,
+                                                   h->d_binom, reinterpret_cast<const float *>(h->d_kfrag), h->d_ins_t,
                                                    h->d_tab_off, x, y);
   DOCI_CUDA(cudaGetLastError());
   return DOCI_OK;
@@ -430,7 +430,7 @@ int launch_pair_ff_no(const doci_ham *h, const double *x, double *y, cudaStream_
     int grid = sms * per_sm;
     if (grid > h->npblocks) grid = h->npblocks;
     sigma_pair_ff_kernel<NO><<<grid, kPairThreads, 0, st>>>(s, reinterpret_cast<const uint2 *>(h->d_pblocks),
-                                                            h->d_rowstart, h->d_binom, h->d_Kmir64, h->d_ins,
+                                                            h->d_rowstart, h->d_binom, h->d_Kmir64, h->d_ins_t,
                                                             h->d_tab_off, xf, y);
     e = cudaGetLastError();
   }
