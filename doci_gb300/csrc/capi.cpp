@@ -289,20 +289,28 @@ int doci_sigma_host(doci_ham *h, const void *x, void *y, int precision) {
   int st = ham_stage(h, bytes);
   if (st) return st;
   // pinned host buffers are read and written by copy kernels through their
-  // device mapping (all SMs on the host link, faster than one copy engine);
+  // device mapping or by the copy engines (both at the host link's rate);
   // pageable ones go through cudaMemcpyAsync
   // (the copy kernels move 4-byte words: a pinned buffer that is not 4-byte
   // aligned takes the cudaMemcpyAsync path too)
   const bool words = (reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) % 4 == 0;
   const void *dx = words ? mapped_host(x) : nullptr;
   void *dy = words ? const_cast<void *>(mapped_host(y)) : nullptr;
-  if (dx) {
-    if ((st = vec_copy(h->d_stage_x, dx, bytes, h->stream))) return st;
+  if (precision == DOCI_FP32 && mapped_host(x) && plan_sigma(h, precision).kind == 6) {
+    // the FP32 pair form overlaps the upload of a pinned x (copy engine, in
+    // pieces) with the units whose rows have arrived
+    st = launch_pair_host(h, static_cast<const float *>(x), static_cast<float *>(h->d_stage_x),
+                          static_cast<float *>(h->d_stage_y), h->stream);
+    if (st) return st;
   } else {
-    DOCI_CUDA(cudaMemcpyAsync(h->d_stage_x, x, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (dx) {
+      if ((st = vec_copy(h->d_stage_x, dx, bytes, h->stream))) return st;
+    } else {
+      DOCI_CUDA(cudaMemcpyAsync(h->d_stage_x, x, bytes, cudaMemcpyHostToDevice, h->stream));
+    }
+    st = launch_sigma(h, h->d_stage_x, h->d_stage_y, precision, h->stream);
+    if (st) return st;
   }
-  st = launch_sigma(h, h->d_stage_x, h->d_stage_y, precision, h->stream);
-  if (st) return st;
   if (dy) {
     if ((st = vec_copy(dy, h->d_stage_y, bytes, h->stream))) return st;
   } else {

@@ -69,13 +69,22 @@ void ham_release(doci_ham *h) {
   if (!h) return;
   cudaStream_t st = h->stream;
   void *bufs[] = {h->d_binom, h->d_Kmir64, h->d_Kmir32, h->d_tab64, h->d_diag, h->d_diag32, h->d_stage_x,
-                  h->d_stage_y, h->d_rows, h->d_rowstart, h->d_pblocks, h->d_kfrag, h->d_tc_err};  // d_rem/d_ins/d_ins_t/d_tab_off are shared (per-process cache)
+                  h->d_stage_y, h->d_rows, h->d_rowstart, h->d_pblocks, h->d_pblocks_host, h->d_kfrag, h->d_tc_err};  // d_rem/d_ins/d_ins_t/d_tab_off are shared (per-process cache)
   for (void *p : bufs) release_async(p, st);
   if (h->h_diag) cudaFreeHost(h->h_diag);
   if (st) {
     cudaStreamSynchronize(st);
     cudaStreamDestroy(st);
   }
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamDestroy(h->copy_stream);
+    for (auto &e : h->chunk_ev)
+      if (e) cudaEventDestroy(e);
+  }
+  h->copy_stream = nullptr;
+  for (auto &e : h->chunk_ev) e = nullptr;
+  h->d_pblocks_host = nullptr;
   h->d_binom = nullptr;
   h->d_Kmir64 = h->d_tab64 = h->d_diag = nullptr;
   h->d_Kmir32 = h->d_diag32 = nullptr;

@@ -101,6 +101,17 @@ struct doci_ham {
   uint32_t *d_pblocks = nullptr;
   int npblocks = 0;
   void *d_kfrag = nullptr;
+  // doci_sigma_host on the FP32 pair form: x crosses the host link in
+  // kHostChunks contiguous pieces (chunk_off) on copy_stream while the units
+  // whose rows have all arrived run: d_pblocks_host holds the same units
+  // grouped by the last piece their rows reach (group g at pgroup_off[g]),
+  // largest first within a group
+  static constexpr int kHostChunks = 8;
+  uint32_t *d_pblocks_host = nullptr;
+  int pgroup_off[kHostChunks + 1] = {};
+  uint64_t chunk_off[kHostChunks + 1] = {};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t chunk_ev[kHostChunks + 1] = {};
 
   // error word of the tensor-core sigma's bounded waits (0 = none)
   int *d_tc_err = nullptr;
@@ -145,6 +156,9 @@ int kernel_blocks(const void *kernel, int threads, size_t dyn, int *blocks);
 // pair-form sigma (sigma_pair.cu), FP32 only
 bool pair_fits(const doci_ham *h);
 int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t s);
+// the same sigma from a pinned host x: the chunked upload into dx overlapped
+// with the unit groups (ham_build_pairs' host grouping); y = dy on stream s
+int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, cudaStream_t s);
 // FP64-accurate pair form in float-float arithmetic (sigma_pair.cu)
 bool pair_ff_fits(const doci_ham *h);
 int launch_pair_ff(const doci_ham *h, const double *x, double *y, cudaStream_t s);

@@ -370,12 +370,43 @@ int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
     flat.push_back(e.second.second);
   }
   h->npblocks = static_cast<int>(bl.size());
+  // host-path grouping: by the last upload piece any row of the unit reaches
+  // (own row R' and hole rows R' u b), stable, so largest first per group
+  constexpr int NC = doci_ham::kHostChunks;
+  for (int k = 0; k <= NC; ++k) h->chunk_off[k] = static_cast<uint64_t>(h->D) * k / NC;
+  auto chunk_of = [&](uint64_t t) {
+    int k = 0;
+    while (k + 1 < NC && h->chunk_off[k + 1] <= t) ++k;
+    return k;
+  };
+  std::vector<std::vector<uint32_t>> groups(NC);
+  for (auto &e : bl) {
+    const uint32_t mask = e.second.second & 0xffffffu;
+    const int kp = static_cast<int>(e.second.second >> 24), jp = N - 1 - kp;
+    int g = 0;
+    if (e.second.first != kNone) g = chunk_of(static_cast<uint64_t>(e.second.first) + binom64(sp, jp + 1) - 1);
+    for (int b = 0; b < na; ++b)
+      if (!(mask >> b & 1u))
+        g = std::max(g, chunk_of(static_cast<uint64_t>(start[mask | (1u << b)]) + binom64(sp, jp) - 1));
+    groups[g].push_back(e.second.first);
+    groups[g].push_back(e.second.second);
+  }
+  std::vector<uint32_t> flat_host;
+  flat_host.reserve(flat.size());
+  h->pgroup_off[0] = 0;
+  for (int g = 0; g < NC; ++g) {
+    flat_host.insert(flat_host.end(), groups[g].begin(), groups[g].end());
+    h->pgroup_off[g + 1] = static_cast<int>(flat_host.size() / 2);
+  }
   DOCI_CUDA(cudaMallocAsync(&h->d_kfrag, ks.size() * sizeof(float), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_kfrag, ks.data(), ks.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   if (!flat.empty()) {
     DOCI_CUDA(cudaMallocAsync(&h->d_pblocks, flat.size() * sizeof(uint32_t), h->stream));
     DOCI_CUDA(cudaMemcpyAsync(h->d_pblocks, flat.data(), flat.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                               h->stream));
+    DOCI_CUDA(cudaMallocAsync(&h->d_pblocks_host, flat_host.size() * sizeof(uint32_t), h->stream));
+    DOCI_CUDA(cudaMemcpyAsync(h->d_pblocks_host, flat_host.data(), flat_host.size() * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice, h->stream));
   }
   DOCI_CUDA(cudaStreamSynchronize(h->stream));
   return DOCI_OK;
@@ -401,6 +432,53 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
                                                    h->d_binom, reinterpret_cast<const float *>(h->d_kfrag), h->d_ins_t,
                                                    h->d_tab_off, x, y);
   DOCI_CUDA(cudaGetLastError());
+  return DOCI_OK;
+}
+
+int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, cudaStream_t st) {
+  if (!pair_fits(h) || !h->d_pblocks_host) return DOCI_ERR_INVALID;
+  constexpr int NC = doci_ham::kHostChunks;
+  if (!h->copy_stream) {
+    DOCI_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    for (auto &e : h->chunk_ev) DOCI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  cudaStream_t cs = h->copy_stream;
+  // the upload starts after the stream's earlier work (dx may still be read)
+  DOCI_CUDA(cudaEventRecord(h->chunk_ev[NC], st));
+  DOCI_CUDA(cudaStreamWaitEvent(cs, h->chunk_ev[NC], 0));
+  for (int k = 0; k < NC; ++k) {
+    const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
+    if (n) DOCI_CUDA(cudaMemcpyAsync(dx + a, hx + a, n * sizeof(float), cudaMemcpyHostToDevice, cs));
+    DOCI_CUDA(cudaEventRecord(h->chunk_ev[k], cs));
+  }
+  const int sms = device_sm_count();
+  int per_sm = 1;
+  const int r = kernel_blocks(reinterpret_cast<const void *>(sigma_pair_kernel), kPairThreads, 0, &per_sm);
+  if (r != DOCI_OK) return r;
+  const uint2 *blocks = reinterpret_cast<const uint2 *>(h->d_pblocks_host);
+  for (int k = 0; k < NC; ++k) {
+    // piece k is in: sigma = diag * x on it (no unit of an earlier group
+    // reaches it), then the units whose rows end in pieces <= k
+    DOCI_CUDA(cudaStreamWaitEvent(st, h->chunk_ev[k], 0));
+    const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
+    if (n) {
+      uint64_t grid = (n + 255) / 256;
+      const uint64_t cap = static_cast<uint64_t>(sms) * 8;
+      if (grid > cap) grid = cap;
+      pair_init_kernel<<<static_cast<unsigned>(grid), 256, 0, st>>>(static_cast<uint32_t>(n), h->d_diag32 + a, dx + a,
+                                                                      dy + a);
+      DOCI_CUDA(cudaGetLastError());
+    }
+    const int nb = h->pgroup_off[k + 1] - h->pgroup_off[k];
+    if (nb > 0) {
+      const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, nb};
+      const int grid = std::min(sms * per_sm, nb);
+      sigma_pair_kernel<<<grid, kPairThreads, 0, st>>>(s, blocks + h->pgroup_off[k], h->d_rowstart, h->d_binom,
+                                                       reinterpret_cast<const float *>(h->d_kfrag), h->d_ins_t,
+                                                       h->d_tab_off, dx, dy);
+      DOCI_CUDA(cudaGetLastError());
+    }
+  }
   return DOCI_OK;
 }
 

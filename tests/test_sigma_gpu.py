@@ -304,6 +304,39 @@ def test_sigma_host_pinned_and_pageable(prec_name, synth, dg):
             assert torch.equal(ys[off:off + D], ref), (pinned, off)
 
 
+@pytest.mark.parametrize("L,N,seed,off", [(22, 11, 31, 0), (24, 12, 30, 3), (20, 7, 33, 1)])
+def test_sigma_host_pair_overlapped_upload(L, N, seed, off, synth, dg):
+    """doci_sigma_host with the FP32 pair form and a pinned x uploads x in
+    pieces on a copy stream while the unit groups whose rows have all arrived
+    run (each group after its piece, sigma = diag * x per piece first): the
+    result matches the oracle within the FP32 tolerance, for an x at an
+    offset inside its buffer too, and a second call on the same handle
+    (reused stream, events and staging) agrees with the first."""
+    torch = torch_cuda()
+    import ctypes as C
+    p = synth(L, N, seed)
+    o = oracle.Ham(p)
+    with dg.Hamiltonian.from_fcidump(p) as h:
+        h.set_sigma_kernel("pair")
+        assert h.sigma_plan(dg.FP32)[0] == 6
+        D = h.D
+        x = np.random.default_rng(seed).standard_normal(D)
+        yr = o.matvec(x)
+        xs = torch.zeros(D + 8, dtype=torch.float32).pin_memory()
+        xs[off:off + D] = torch.from_numpy(x.astype(np.float32))
+        ys = torch.full((D + 8,), float("nan"), dtype=torch.float32).pin_memory()
+        lib = dg.lib()
+        outs = []
+        for _ in range(2):
+            st = lib.doci_sigma_host(h.handle, C.c_void_p(xs[off:].data_ptr()), C.c_void_p(ys[off:].data_ptr()),
+                                     dg.FP32)
+            assert st == 0
+            outs.append(ys[off:off + D].numpy().astype(np.float64).copy())
+        for y in outs:
+            assert np.abs(y - yr).max() <= TOL32 * np.abs(yr).max()
+        assert np.abs(outs[0] - outs[1]).max() <= TOL32 * np.abs(yr).max()
+
+
 def test_autotune_keeps_parity(synth, dg):
     """doci_ham_autotune picks a path that fits, the plan reports it, sigma on
     the tuned path still matches the oracle, and a second handle of the same
