@@ -297,11 +297,18 @@ int doci_sigma_host(doci_ham *h, const void *x, void *y, int precision) {
   const void *dx = words ? mapped_host(x) : nullptr;
   void *dy = words ? const_cast<void *>(mapped_host(y)) : nullptr;
   if (precision == DOCI_FP32 && mapped_host(x) && plan_sigma(h, precision).kind == 6) {
-    // the FP32 pair form overlaps the upload of a pinned x (copy engine, in
-    // pieces) with the units whose rows have arrived
+    // the FP32 pair form overlaps the copies of a pinned x (and a pinned y)
+    // with the sigma: pieces go up and come down on the copy engines while
+    // the unit groups run
+    const bool y_pinned = mapped_host(y) != nullptr;
     st = launch_pair_host(h, static_cast<const float *>(x), static_cast<float *>(h->d_stage_x),
-                          static_cast<float *>(h->d_stage_y), h->stream);
+                          static_cast<float *>(h->d_stage_y), y_pinned ? static_cast<float *>(y) : nullptr,
+                          h->stream);
     if (st) return st;
+    if (y_pinned) {
+      DOCI_CUDA(cudaStreamSynchronize(h->stream));
+      return ham_device_error(h, h->stream);
+    }
   } else {
     if (dx) {
       if ((st = vec_copy(h->d_stage_x, dx, bytes, h->stream))) return st;

@@ -79,12 +79,22 @@ void ham_release(doci_ham *h) {
   if (h->copy_stream) {
     cudaStreamSynchronize(h->copy_stream);
     cudaStreamDestroy(h->copy_stream);
-    for (auto &e : h->chunk_ev)
-      if (e) cudaEventDestroy(e);
+  }
+  for (cudaEvent_t *e : {&h->start_ev, &h->end_ev}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
+  for (auto &e : h->up_ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+  for (auto &e : h->down_ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
   }
   h->copy_stream = nullptr;
-  for (auto &e : h->chunk_ev) e = nullptr;
   h->d_pblocks_host = nullptr;
+  h->host_groups.clear();
   h->d_binom = nullptr;
   h->d_Kmir64 = h->d_tab64 = h->d_diag = nullptr;
   h->d_Kmir32 = h->d_diag32 = nullptr;

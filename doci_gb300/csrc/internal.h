@@ -101,17 +101,24 @@ struct doci_ham {
   uint32_t *d_pblocks = nullptr;
   int npblocks = 0;
   void *d_kfrag = nullptr;
-  // doci_sigma_host on the FP32 pair form: x crosses the host link in
-  // kHostChunks contiguous pieces (chunk_off) on copy_stream while the units
-  // whose rows have all arrived run: d_pblocks_host holds the same units
-  // grouped by the last piece their rows reach (group g at pgroup_off[g]),
-  // largest first within a group
+  // doci_sigma_host on the FP32 pair form: x and sigma cross the host link
+  // in kHostChunks contiguous pieces (chunk_off) on copy_stream while the
+  // pair units run in groups (sigma_pair.cu, host_schedule): a group starts
+  // once the last piece its rows reach is up, and a piece of sigma goes down
+  // once the last group touching it is done.  d_pblocks_host holds the units
+  // in group order, largest first within a group.
   static constexpr int kHostChunks = 8;
+  struct HostGroup {
+    int first, count;          // units [first, first + count) of d_pblocks_host
+    int need;                  // last upload piece its rows reach
+    uint32_t init_mask;        // pieces whose sigma = diag * x pass runs first
+    uint32_t down_mask;        // pieces final after it
+  };
   uint32_t *d_pblocks_host = nullptr;
-  int pgroup_off[kHostChunks + 1] = {};
+  std::vector<HostGroup> host_groups;
   uint64_t chunk_off[kHostChunks + 1] = {};
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t chunk_ev[kHostChunks + 1] = {};
+  cudaEvent_t up_ev[kHostChunks] = {}, down_ev[kHostChunks] = {}, start_ev = nullptr, end_ev = nullptr;
 
   // error word of the tensor-core sigma's bounded waits (0 = none)
   int *d_tc_err = nullptr;
@@ -156,9 +163,10 @@ int kernel_blocks(const void *kernel, int threads, size_t dyn, int *blocks);
 // pair-form sigma (sigma_pair.cu), FP32 only
 bool pair_fits(const doci_ham *h);
 int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t s);
-// the same sigma from a pinned host x: the chunked upload into dx overlapped
-// with the unit groups (ham_build_pairs' host grouping); y = dy on stream s
-int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, cudaStream_t s);
+// the same sigma from a pinned host x: the upload into dx in pieces,
+// overlapped with the unit groups; y = dy on stream s, and, for a pinned hy,
+// the pieces of dy copied to hy as they become final (all done when s is)
+int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *hy, cudaStream_t s);
 // FP64-accurate pair form in float-float arithmetic (sigma_pair.cu)
 bool pair_ff_fits(const doci_ham *h);
 int launch_pair_ff(const doci_ham *h, const double *x, double *y, cudaStream_t s);

@@ -27,6 +27,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <random>
 #include <vector>
 
 #include "addressing.cuh"
@@ -342,6 +344,121 @@ bool pair_fits(const doci_ham *h) {
   return static_cast<size_t>(h->max_row) * sizeof(float) <= 100 * 1024;
 }
 
+namespace {
+
+struct HostUnit {
+  uint32_t own, word;  // as in d_pblocks
+  uint64_t sets;       // (N-1)-pair sets of the unit
+  uint32_t touched;    // pieces its rows reach
+};
+
+// Order of the unit groups for the host-buffer sigma.  Units are grouped by
+// (first, last) piece their rows reach; a group can start once its last
+// piece is up (pieces go up in order), and a piece of sigma can go down once
+// every group reaching it is done.  The order minimises the modelled end of
+// the download: GB300 measurements, upload 211 GB/s, download 193 GB/s, the
+// pair kernel 0.061 ns per set; a deterministic local search (random pair
+// swaps from the order by last piece) over the at most 36 groups.  The model
+// only orders the work: every order gives the same sigma.
+void host_schedule(doci_ham *h, const std::vector<HostUnit> &hu, std::vector<uint32_t> &flat) {
+  constexpr int NC = doci_ham::kHostChunks;
+  struct Cls {
+    double sets = 0;
+    int first = NC, last = -1;
+    uint32_t mask = 0;
+    std::vector<const HostUnit *> units;
+  };
+  std::map<std::pair<int, int>, Cls> by;
+  for (const HostUnit &u : hu) {
+    if (!u.touched) continue;
+    const int lo = __builtin_ctz(u.touched), hi = 31 - __builtin_clz(u.touched);
+    Cls &c = by[{lo, hi}];
+    c.sets += static_cast<double>(u.sets);
+    c.first = lo;
+    c.last = hi;
+    c.mask |= u.touched;
+    c.units.push_back(&u);
+  }
+  std::vector<Cls> cls;
+  for (auto &kv : by) cls.push_back(std::move(kv.second));
+  double total = 0;
+  for (auto &c : cls) total += c.sets;
+  const double piece_bytes = static_cast<double>(h->D) * sizeof(float) / NC;
+  const double t_up = piece_bytes / 211e9, t_down = piece_bytes / 193e9, t_set = 0.061e-9;
+  auto model = [&](const std::vector<int> &order) {
+    double t = 0, ready[NC];
+    for (double &r : ready) r = -1;
+    for (int i : order) {
+      const Cls &c = cls[i];
+      t = std::max(t, (c.last + 1) * t_up) + c.sets * t_set;
+      for (int k = 0; k < NC; ++k)
+        if (c.mask >> k & 1u) ready[k] = t;
+    }
+    t = std::max(t, NC * t_up);
+    for (double &r : ready)
+      if (r < 0) r = t;
+    std::sort(ready, ready + NC);
+    double d = 0;
+    for (double r : ready) d = std::max(d, r) + t_down;
+    return d;
+  };
+  std::vector<int> order(cls.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int>(i);
+  std::sort(order.begin(), order.end(), [&](int a, int b) {
+    return cls[a].last != cls[b].last ? cls[a].last < cls[b].last : cls[a].first < cls[b].first;
+  });
+  double best = model(order);
+  if (order.size() > 1) {
+    std::mt19937 rng(12345);
+    std::uniform_int_distribution<size_t> pick(0, order.size() - 1);
+    for (int it = 0; it < 20000; ++it) {
+      std::vector<int> o = order;
+      std::swap(o[pick(rng)], o[pick(rng)]);
+      const double v = model(o);
+      if (v <= best) {
+        best = v;
+        order.swap(o);
+      }
+    }
+  }
+  h->host_groups.clear();
+  flat.clear();
+  uint32_t inited = 0;
+  int last_of[NC];
+  for (int &l : last_of) l = -1;
+  for (size_t g = 0; g < order.size(); ++g)
+    for (int k = 0; k < NC; ++k)
+      if (cls[order[g]].mask >> k & 1u) last_of[k] = static_cast<int>(g);
+  for (size_t g = 0; g < order.size(); ++g) {
+    const Cls &c = cls[order[g]];
+    doci_ham::HostGroup hg{};
+    hg.first = static_cast<int>(flat.size() / 2);
+    for (const HostUnit *u : c.units) {
+      flat.push_back(u->own);
+      flat.push_back(u->word);
+    }
+    hg.count = static_cast<int>(c.units.size());
+    hg.need = c.last;
+    const uint32_t upto = (c.last + 1 >= 32) ? 0xffffffffu : ((1u << (c.last + 1)) - 1u);
+    hg.init_mask = upto & ~inited;
+    inited |= hg.init_mask;
+    for (int k = 0; k < NC; ++k)
+      if (last_of[k] == static_cast<int>(g)) hg.down_mask |= 1u << k;
+    h->host_groups.push_back(hg);
+  }
+  // pieces no unit reaches: their diagonal pass and download close the call
+  doci_ham::HostGroup tail{};
+  tail.first = static_cast<int>(flat.size() / 2);
+  tail.count = 0;
+  tail.need = NC - 1;
+  tail.init_mask = ((1u << NC) - 1u) & ~inited;
+  for (int k = 0; k < NC; ++k)
+    if (last_of[k] < 0) tail.down_mask |= 1u << k;
+  if (tail.init_mask || tail.down_mask) h->host_groups.push_back(tail);
+}
+
+}  // namespace
+
 int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
   const int L = h->L, N = h->N, sp = h->split, na = L - sp;
   // K (mirrored orbitals, zero outside 0..L-1) split into TF32 high and low
@@ -370,8 +487,7 @@ int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
     flat.push_back(e.second.second);
   }
   h->npblocks = static_cast<int>(bl.size());
-  // host-path grouping: by the last upload piece any row of the unit reaches
-  // (own row R' and hole rows R' u b), stable, so largest first per group
+  // host-buffer path: pieces of the vector and the group schedule
   constexpr int NC = doci_ham::kHostChunks;
   for (int k = 0; k <= NC; ++k) h->chunk_off[k] = static_cast<uint64_t>(h->D) * k / NC;
   auto chunk_of = [&](uint64_t t) {
@@ -379,25 +495,22 @@ int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
     while (k + 1 < NC && h->chunk_off[k + 1] <= t) ++k;
     return k;
   };
-  std::vector<std::vector<uint32_t>> groups(NC);
+  std::vector<HostUnit> hu;
+  hu.reserve(bl.size());
   for (auto &e : bl) {
     const uint32_t mask = e.second.second & 0xffffffu;
     const int kp = static_cast<int>(e.second.second >> 24), jp = N - 1 - kp;
-    int g = 0;
-    if (e.second.first != kNone) g = chunk_of(static_cast<uint64_t>(e.second.first) + binom64(sp, jp + 1) - 1);
+    uint32_t touched = 0;
+    auto row = [&](uint64_t rs, uint64_t len) {
+      for (int c = chunk_of(rs); c <= chunk_of(rs + len - 1); ++c) touched |= 1u << c;
+    };
+    if (e.second.first != kNone) row(e.second.first, binom64(sp, jp + 1));
     for (int b = 0; b < na; ++b)
-      if (!(mask >> b & 1u))
-        g = std::max(g, chunk_of(static_cast<uint64_t>(start[mask | (1u << b)]) + binom64(sp, jp) - 1));
-    groups[g].push_back(e.second.first);
-    groups[g].push_back(e.second.second);
+      if (!(mask >> b & 1u)) row(start[mask | (1u << b)], binom64(sp, jp));
+    hu.push_back({e.second.first, e.second.second, binom64(sp, jp), touched});
   }
   std::vector<uint32_t> flat_host;
-  flat_host.reserve(flat.size());
-  h->pgroup_off[0] = 0;
-  for (int g = 0; g < NC; ++g) {
-    flat_host.insert(flat_host.end(), groups[g].begin(), groups[g].end());
-    h->pgroup_off[g + 1] = static_cast<int>(flat_host.size() / 2);
-  }
+  host_schedule(h, hu, flat_host);
   DOCI_CUDA(cudaMallocAsync(&h->d_kfrag, ks.size() * sizeof(float), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_kfrag, ks.data(), ks.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   if (!flat.empty()) {
@@ -435,33 +548,41 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
   return DOCI_OK;
 }
 
-int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, cudaStream_t st) {
-  if (!pair_fits(h) || !h->d_pblocks_host) return DOCI_ERR_INVALID;
+int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *hy, cudaStream_t st) {
+  if (!pair_fits(h) || !h->d_pblocks_host || h->host_groups.empty()) return DOCI_ERR_INVALID;
   constexpr int NC = doci_ham::kHostChunks;
   if (!h->copy_stream) {
     DOCI_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
-    for (auto &e : h->chunk_ev) DOCI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &e : h->up_ev) DOCI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &e : h->down_ev) DOCI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    DOCI_CUDA(cudaEventCreateWithFlags(&h->start_ev, cudaEventDisableTiming));
+    DOCI_CUDA(cudaEventCreateWithFlags(&h->end_ev, cudaEventDisableTiming));
   }
   cudaStream_t cs = h->copy_stream;
   // the upload starts after the stream's earlier work (dx may still be read)
-  DOCI_CUDA(cudaEventRecord(h->chunk_ev[NC], st));
-  DOCI_CUDA(cudaStreamWaitEvent(cs, h->chunk_ev[NC], 0));
+  DOCI_CUDA(cudaEventRecord(h->start_ev, st));
+  DOCI_CUDA(cudaStreamWaitEvent(cs, h->start_ev, 0));
   for (int k = 0; k < NC; ++k) {
     const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
     if (n) DOCI_CUDA(cudaMemcpyAsync(dx + a, hx + a, n * sizeof(float), cudaMemcpyHostToDevice, cs));
-    DOCI_CUDA(cudaEventRecord(h->chunk_ev[k], cs));
+    DOCI_CUDA(cudaEventRecord(h->up_ev[k], cs));
   }
   const int sms = device_sm_count();
   int per_sm = 1;
   const int r = kernel_blocks(reinterpret_cast<const void *>(sigma_pair_kernel), kPairThreads, 0, &per_sm);
   if (r != DOCI_OK) return r;
   const uint2 *blocks = reinterpret_cast<const uint2 *>(h->d_pblocks_host);
-  for (int k = 0; k < NC; ++k) {
-    // piece k is in: sigma = diag * x on it (no unit of an earlier group
-    // reaches it), then the units whose rows end in pieces <= k
-    DOCI_CUDA(cudaStreamWaitEvent(st, h->chunk_ev[k], 0));
-    const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
-    if (n) {
+  int waited = -1;
+  for (const doci_ham::HostGroup &g : h->host_groups) {
+    if (g.need > waited) {  // pieces go up in order: waiting for the last one covers the rest
+      DOCI_CUDA(cudaStreamWaitEvent(st, h->up_ev[g.need], 0));
+      waited = g.need;
+    }
+    // sigma = diag * x on the pieces this group is the first to reach
+    for (int k = 0; k < NC; ++k) {
+      if (!(g.init_mask >> k & 1u)) continue;
+      const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
+      if (!n) continue;
       uint64_t grid = (n + 255) / 256;
       const uint64_t cap = static_cast<uint64_t>(sms) * 8;
       if (grid > cap) grid = cap;
@@ -469,15 +590,27 @@ int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, cudaStr
                                                                       dy + a);
       DOCI_CUDA(cudaGetLastError());
     }
-    const int nb = h->pgroup_off[k + 1] - h->pgroup_off[k];
-    if (nb > 0) {
-      const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, nb};
-      const int grid = std::min(sms * per_sm, nb);
-      sigma_pair_kernel<<<grid, kPairThreads, 0, st>>>(s, blocks + h->pgroup_off[k], h->d_rowstart, h->d_binom,
+    if (g.count > 0) {
+      const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, g.count};
+      const int grid = std::min(sms * per_sm, g.count);
+      sigma_pair_kernel<<<grid, kPairThreads, 0, st>>>(s, blocks + g.first, h->d_rowstart, h->d_binom,
                                                        reinterpret_cast<const float *>(h->d_kfrag), h->d_ins_t,
                                                        h->d_tab_off, dx, dy);
       DOCI_CUDA(cudaGetLastError());
     }
+    if (!hy) continue;
+    // pieces no later group reaches go down now, behind the upload
+    for (int k = 0; k < NC; ++k) {
+      if (!(g.down_mask >> k & 1u)) continue;
+      const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
+      DOCI_CUDA(cudaEventRecord(h->down_ev[k], st));
+      DOCI_CUDA(cudaStreamWaitEvent(cs, h->down_ev[k], 0));
+      if (n) DOCI_CUDA(cudaMemcpyAsync(hy + a, dy + a, n * sizeof(float), cudaMemcpyDeviceToHost, cs));
+    }
+  }
+  if (hy) {
+    DOCI_CUDA(cudaEventRecord(h->end_ev, cs));
+    DOCI_CUDA(cudaStreamWaitEvent(st, h->end_ev, 0));
   }
   return DOCI_OK;
 }
