@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the FP64-accurate sigma (device-resident and end to end) of an FP32 run")
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge measurement")
     ap.add_argument("--converge-repeats", type=int, default=20,
                     help="mixed solves of the L=28 N=14 Hamiltonian for time-to-converge p50/p99 (0 = none)")
@@ -187,6 +189,43 @@ class ClockSampler:
             return None
         return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sms)}
+
+
+def fp64_like_for_like(h, D, dg, torch, steps: int):
+    """The FP64-accurate sigma on the same Hamiltonian (the reference computes
+    in FP64): device-resident (CUDA events on its stream, after a warm-up) and
+    end to end through doci_sigma_host on pinned FP64 host buffers (copies
+    inside each call; wall clock over the calls after a warm-up call)."""
+    import ctypes as C
+    kind, _ = h.sigma_plan(dg.FP64)
+    x = torch.randn(D, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(77))
+    y = torch.empty_like(x)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    h.sigma_device(x.data_ptr(), y.data_ptr(), dg.FP64, sp)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        h.sigma_device(x.data_ptr(), y.data_ptr(), dg.FP64, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    del x, y
+    torch.cuda.empty_cache()
+    hx = torch.randn(D, dtype=torch.float64, generator=torch.Generator().manual_seed(6)).pin_memory()
+    hy = torch.empty(D, dtype=torch.float64).pin_memory()
+    lib = dg.lib()
+    assert lib.doci_sigma_host(h.handle, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()), dg.FP64) == 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        assert lib.doci_sigma_host(h.handle, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()), dg.FP64) == 0
+    te = (time.perf_counter() - t0) / steps
+    return {"value": round(D / ms / 1e6, 4), "unit": UNIT, "sigma_ms": round(ms, 3),
+            "sigma_kernel": KERNEL_NAMES.get(kind, kind), "dtype": "f64 (float-float pair form)" if kind == 9 else "f64",
+            "e2e": {"value": round(D / te / 1e9, 4), "unit": UNIT, "ms_per_call": round(te * 1e3, 3),
+                    "h2d_bytes_per_step": D * 8, "d2h_bytes_per_step": D * 8,
+                    "call": "doci_sigma_host FP64 (C ABI, pinned host buffers)", "steps": steps}}
 
 
 def converge_report(h, max_vec: int, mixed_tol: float, threshold: float = 1e-8):
@@ -603,6 +642,9 @@ def main():
         e2e = {"value": round(replica_gdets(D, a.e2e_steps, ws, te), 4), "unit": UNIT,
                "h2d_bytes_per_step": D * esize, "d2h_bytes_per_step": D * esize,
                "call": "doci_sigma_host (C ABI, pinned host buffers)", "steps": a.e2e_steps}
+    fp64 = None
+    if prec == dg.FP32 and nv == 1 and not a.no_fp64 and rank == 0:
+        fp64 = fp64_like_for_like(h, D, dg, torch, a.e2e_steps)
     conv = None
     if not a.no_converge and rank == 0:
         del x, y
@@ -629,7 +671,7 @@ def main():
                            "parallelism": f"replicas x{ws}"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": a.steps * launches_per_step,
                 "sigma_kernel": KERNEL_NAMES.get(plan_kind, plan_kind),
-                "clocks": clk, "time_to_converge": conv, "impl": "ours"}
+                "clocks": clk, "time_to_converge": conv, "fp64": fp64, "impl": "ours"}
         print(json.dumps(line), flush=True)
     h.close()
     if ws > 1:

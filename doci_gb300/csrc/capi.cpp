@@ -296,14 +296,23 @@ int doci_sigma_host(doci_ham *h, const void *x, void *y, int precision) {
   const bool words = (reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) % 4 == 0;
   const void *dx = words ? mapped_host(x) : nullptr;
   void *dy = words ? const_cast<void *>(mapped_host(y)) : nullptr;
-  if (precision == DOCI_FP32 && mapped_host(x) && plan_sigma(h, precision).kind == 6) {
-    // the FP32 pair form overlaps the copies of a pinned x (and a pinned y)
-    // with the sigma: pieces go up and come down on the copy engines while
-    // the unit groups run
+  const int kind = plan_sigma(h, precision).kind;
+  const bool sched = h->d_pblocks_host && !h->host_groups.empty();
+  if (sched && ((precision == DOCI_FP32 && kind == 6 && pair_fits(h)) ||
+                (precision == DOCI_FP64 && kind == 9 && pair_ff_fits(h)))) {
+    // the pair forms overlap the copies with the sigma: pieces of x go up and
+    // pieces of y come down on the copy engines while the unit groups run (a
+    // pageable y is copied after the sigma: a copy into pageable memory can
+    // hold the calling thread until it is done)
     const bool y_pinned = mapped_host(y) != nullptr;
-    st = launch_pair_host(h, static_cast<const float *>(x), static_cast<float *>(h->d_stage_x),
-                          static_cast<float *>(h->d_stage_y), y_pinned ? static_cast<float *>(y) : nullptr,
-                          h->stream);
+    if (precision == DOCI_FP32)
+      st = launch_pair_host(h, static_cast<const float *>(x), static_cast<float *>(h->d_stage_x),
+                            static_cast<float *>(h->d_stage_y), y_pinned ? static_cast<float *>(y) : nullptr,
+                            h->stream);
+    else
+      st = launch_pair_ff_host(h, static_cast<const double *>(x), static_cast<double *>(h->d_stage_x),
+                               static_cast<double *>(h->d_stage_y), y_pinned ? static_cast<double *>(y) : nullptr,
+                               h->stream);
     if (st) return st;
     if (y_pinned) {
       DOCI_CUDA(cudaStreamSynchronize(h->stream));

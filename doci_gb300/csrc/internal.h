@@ -170,6 +170,8 @@ int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *
 // FP64-accurate pair form in float-float arithmetic (sigma_pair.cu)
 bool pair_ff_fits(const doci_ham *h);
 int launch_pair_ff(const doci_ham *h, const double *x, double *y, cudaStream_t s);
+// its host-buffer form on the same piece and group schedule as launch_pair_host
+int launch_pair_ff_host(doci_ham *h, const double *hx, double *dx, double *dy, double *hy, cudaStream_t s);
 // tensor-core pair form (sigma_tc.cu), FP32 only, sm_103a; x 16-byte aligned.
 // A device wait that runs out writes a nonzero code to *d_err (spin_limit:
 // try_wait iterations per wait).

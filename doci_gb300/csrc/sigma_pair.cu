@@ -548,8 +548,15 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
   return DOCI_OK;
 }
 
-int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *hy, cudaStream_t st) {
-  if (!pair_fits(h) || !h->d_pblocks_host || h->host_groups.empty()) return DOCI_ERR_INVALID;
+namespace {
+
+// One host-buffer sigma on the group schedule of host_schedule: the pieces
+// of hx go up in order on the copy stream; on st, per group, init(a, n) runs
+// the diagonal pass of each piece the group is the first to reach and
+// group(first, count) its units; with hy, each piece of dy goes down (copy
+// stream) once no later group reaches it, and st waits for the last one.
+template <typename T, typename Init, typename Group>
+int run_host_schedule(doci_ham *h, const T *hx, T *dx, T *dy, T *hy, cudaStream_t st, Init init, Group group) {
   constexpr int NC = doci_ham::kHostChunks;
   if (!h->copy_stream) {
     DOCI_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
@@ -564,39 +571,26 @@ int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *
   DOCI_CUDA(cudaStreamWaitEvent(cs, h->start_ev, 0));
   for (int k = 0; k < NC; ++k) {
     const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
-    if (n) DOCI_CUDA(cudaMemcpyAsync(dx + a, hx + a, n * sizeof(float), cudaMemcpyHostToDevice, cs));
+    if (n) DOCI_CUDA(cudaMemcpyAsync(dx + a, hx + a, n * sizeof(T), cudaMemcpyHostToDevice, cs));
     DOCI_CUDA(cudaEventRecord(h->up_ev[k], cs));
   }
-  const int sms = device_sm_count();
-  int per_sm = 1;
-  const int r = kernel_blocks(reinterpret_cast<const void *>(sigma_pair_kernel), kPairThreads, 0, &per_sm);
-  if (r != DOCI_OK) return r;
-  const uint2 *blocks = reinterpret_cast<const uint2 *>(h->d_pblocks_host);
   int waited = -1;
   for (const doci_ham::HostGroup &g : h->host_groups) {
     if (g.need > waited) {  // pieces go up in order: waiting for the last one covers the rest
       DOCI_CUDA(cudaStreamWaitEvent(st, h->up_ev[g.need], 0));
       waited = g.need;
     }
-    // sigma = diag * x on the pieces this group is the first to reach
     for (int k = 0; k < NC; ++k) {
       if (!(g.init_mask >> k & 1u)) continue;
       const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
-      if (!n) continue;
-      uint64_t grid = (n + 255) / 256;
-      const uint64_t cap = static_cast<uint64_t>(sms) * 8;
-      if (grid > cap) grid = cap;
-      pair_init_kernel<<<static_cast<unsigned>(grid), 256, 0, st>>>(static_cast<uint32_t>(n), h->d_diag32 + a, dx + a,
-                                                                      dy + a);
-      DOCI_CUDA(cudaGetLastError());
+      if (n) {
+        const int r = init(a, n);
+        if (r != DOCI_OK) return r;
+      }
     }
     if (g.count > 0) {
-      const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, g.count};
-      const int grid = std::min(sms * per_sm, g.count);
-      sigma_pair_kernel<<<grid, kPairThreads, 0, st>>>(s, blocks + g.first, h->d_rowstart, h->d_binom,
-                                                       reinterpret_cast<const float *>(h->d_kfrag), h->d_ins_t,
-                                                       h->d_tab_off, dx, dy);
-      DOCI_CUDA(cudaGetLastError());
+      const int r = group(g.first, g.count);
+      if (r != DOCI_OK) return r;
     }
     if (!hy) continue;
     // pieces no later group reaches go down now, behind the upload
@@ -605,7 +599,7 @@ int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *
       const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
       DOCI_CUDA(cudaEventRecord(h->down_ev[k], st));
       DOCI_CUDA(cudaStreamWaitEvent(cs, h->down_ev[k], 0));
-      if (n) DOCI_CUDA(cudaMemcpyAsync(hy + a, dy + a, n * sizeof(float), cudaMemcpyDeviceToHost, cs));
+      if (n) DOCI_CUDA(cudaMemcpyAsync(hy + a, dy + a, n * sizeof(T), cudaMemcpyDeviceToHost, cs));
     }
   }
   if (hy) {
@@ -613,6 +607,76 @@ int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *
     DOCI_CUDA(cudaStreamWaitEvent(st, h->end_ev, 0));
   }
   return DOCI_OK;
+}
+
+unsigned init_grid(uint64_t n) {
+  const uint64_t cap = static_cast<uint64_t>(device_sm_count()) * 8;
+  return static_cast<unsigned>(std::min((n + 255) / 256, cap));
+}
+
+template <int NO>
+int launch_pair_ff_host_no(doci_ham *h, const double *hx, double *dx, double *dy, double *hy, cudaStream_t st) {
+  int per_sm = 1;
+  int r = kernel_blocks(reinterpret_cast<const void *>(sigma_pair_ff_kernel<NO>), kPairThreads, 0, &per_sm);
+  if (r != DOCI_OK) return r;
+  const int slots = device_sm_count() * per_sm;
+  ff *xf = nullptr;
+  DOCI_CUDA(cudaMallocAsync(&xf, sizeof(ff) * static_cast<size_t>(h->D), st));
+  const uint2 *blocks = reinterpret_cast<const uint2 *>(h->d_pblocks_host);
+  r = run_host_schedule<double>(
+      h, hx, dx, dy, hy, st,
+      [&](uint64_t a, uint64_t n) {
+        pair_init64_kernel<<<init_grid(n), 256, 0, st>>>(static_cast<uint32_t>(n), h->d_diag + a, dx + a, dy + a,
+                                                          xf + a);
+        DOCI_CUDA(cudaGetLastError());
+        return static_cast<int>(DOCI_OK);
+      },
+      [&](int first, int count) {
+        const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, count};
+        sigma_pair_ff_kernel<NO><<<std::min(slots, count), kPairThreads, 0, st>>>(
+            s, blocks + first, h->d_rowstart, h->d_binom, h->d_Kmir64, h->d_ins_t, h->d_tab_off, xf, dy);
+        DOCI_CUDA(cudaGetLastError());
+        return static_cast<int>(DOCI_OK);
+      });
+  const cudaError_t ef = cudaFreeAsync(xf, st);
+  if (r != DOCI_OK) return r;
+  DOCI_CUDA(ef);
+  return DOCI_OK;
+}
+
+}  // namespace
+
+int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *hy, cudaStream_t st) {
+  if (!pair_fits(h) || !h->d_pblocks_host || h->host_groups.empty()) return DOCI_ERR_INVALID;
+  int per_sm = 1;
+  const int r = kernel_blocks(reinterpret_cast<const void *>(sigma_pair_kernel), kPairThreads, 0, &per_sm);
+  if (r != DOCI_OK) return r;
+  const int slots = device_sm_count() * per_sm;
+  const uint2 *blocks = reinterpret_cast<const uint2 *>(h->d_pblocks_host);
+  return run_host_schedule<float>(
+      h, hx, dx, dy, hy, st,
+      [&](uint64_t a, uint64_t n) {
+        pair_init_kernel<<<init_grid(n), 256, 0, st>>>(static_cast<uint32_t>(n), h->d_diag32 + a, dx + a, dy + a);
+        DOCI_CUDA(cudaGetLastError());
+        return static_cast<int>(DOCI_OK);
+      },
+      [&](int first, int count) {
+        const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, count};
+        sigma_pair_kernel<<<std::min(slots, count), kPairThreads, 0, st>>>(
+            s, blocks + first, h->d_rowstart, h->d_binom, reinterpret_cast<const float *>(h->d_kfrag), h->d_ins_t,
+            h->d_tab_off, dx, dy);
+        DOCI_CUDA(cudaGetLastError());
+        return static_cast<int>(DOCI_OK);
+      });
+}
+
+int launch_pair_ff_host(doci_ham *h, const double *hx, double *dx, double *dy, double *hy, cudaStream_t st) {
+  if (!pair_ff_fits(h) || !h->d_pblocks_host || h->host_groups.empty()) return DOCI_ERR_INVALID;
+  const int no = h->L - h->N + 1;
+  if (no <= 8) return launch_pair_ff_host_no<8>(h, hx, dx, dy, hy, st);
+  if (no <= 17) return launch_pair_ff_host_no<17>(h, hx, dx, dy, hy, st);
+  if (no <= 24) return launch_pair_ff_host_no<24>(h, hx, dx, dy, hy, st);
+  return launch_pair_ff_host_no<32>(h, hx, dx, dy, hy, st);
 }
 
 bool pair_ff_fits(const doci_ham *h) { return pair_fits(h) && h->L - h->N + 1 <= 32; }

@@ -213,9 +213,9 @@ int doci_ham_autotune(doci_ham *ham, int precision, int nvec, int *choice);
 int doci_sigma_plan(const doci_ham *ham, int precision, int *kind, int *launches);
 
 /* Same on host buffers; copies in and out inside the call, synchronous.  On
- * the FP32 pair form (kind 6) a pinned (page-locked) x is uploaded, and a
- * pinned y downloaded, in pieces on the handle's own copy stream, overlapped
- * with the sigma. */
+ * the pair forms (kinds 6 and 9) x is uploaded, and a pinned (page-locked) y
+ * downloaded, in pieces on the handle's own copy stream, overlapped with the
+ * sigma. */
 int doci_sigma_host(doci_ham *ham, const void *x, void *y, int precision);
 
 /* Lexical addressing on the device: bitstrings of determinants

@@ -304,37 +304,44 @@ def test_sigma_host_pinned_and_pageable(prec_name, synth, dg):
             assert torch.equal(ys[off:off + D], ref), (pinned, off)
 
 
-@pytest.mark.parametrize("L,N,seed,off", [(22, 11, 31, 0), (24, 12, 30, 3), (20, 7, 33, 1)])
-def test_sigma_host_pair_overlapped_upload(L, N, seed, off, synth, dg):
-    """doci_sigma_host with the FP32 pair form and a pinned x uploads x in
-    pieces on a copy stream while the unit groups whose rows have all arrived
-    run (each group after its piece, sigma = diag * x per piece first): the
-    result matches the oracle within the FP32 tolerance, for an x at an
-    offset inside its buffer too, and a second call on the same handle
-    (reused stream, events and staging) agrees with the first."""
+@pytest.mark.parametrize("prec_name,kernel", [("FP32", "pair"), ("FP64", "rowff")])
+@pytest.mark.parametrize("L,N,seed,off,pinned", [(22, 11, 31, 0, True), (24, 12, 30, 3, True), (20, 7, 33, 1, True),
+                                                 (22, 11, 34, 0, False)])
+def test_sigma_host_pair_overlapped_copies(prec_name, kernel, L, N, seed, off, pinned, synth, dg):
+    """doci_sigma_host on the pair forms (FP32 kind 6, FP64-accurate kind 9)
+    uploads x in pieces on a copy stream while the unit groups whose rows
+    have all arrived run (each piece's diagonal pass before the first group
+    reaching it) and downloads a pinned y piece by piece as no later group
+    reaches it: the result matches the oracle within the precision's
+    tolerance, for buffers at an offset and for pageable ones, and a second
+    call on the same handle (reused stream, events, staging) agrees with the
+    first."""
     torch = torch_cuda()
     import ctypes as C
+    prec = getattr(dg, prec_name)
+    tdt, tol = (torch.float32, TOL32) if prec == dg.FP32 else (torch.float64, TOL64)
     p = synth(L, N, seed)
     o = oracle.Ham(p)
     with dg.Hamiltonian.from_fcidump(p) as h:
-        h.set_sigma_kernel("pair")
-        assert h.sigma_plan(dg.FP32)[0] == 6
+        h.set_sigma_kernel(kernel)
+        assert h.sigma_plan(prec)[0] == (6 if prec == dg.FP32 else 9)
         D = h.D
         x = np.random.default_rng(seed).standard_normal(D)
         yr = o.matvec(x)
-        xs = torch.zeros(D + 8, dtype=torch.float32).pin_memory()
-        xs[off:off + D] = torch.from_numpy(x.astype(np.float32))
-        ys = torch.full((D + 8,), float("nan"), dtype=torch.float32).pin_memory()
+        xs = torch.zeros(D + 8, dtype=tdt)
+        ys = torch.full((D + 8,), float("nan"), dtype=tdt)
+        if pinned:
+            xs, ys = xs.pin_memory(), ys.pin_memory()
+        xs[off:off + D] = torch.from_numpy(x).to(tdt)
         lib = dg.lib()
         outs = []
         for _ in range(2):
-            st = lib.doci_sigma_host(h.handle, C.c_void_p(xs[off:].data_ptr()), C.c_void_p(ys[off:].data_ptr()),
-                                     dg.FP32)
+            st = lib.doci_sigma_host(h.handle, C.c_void_p(xs[off:].data_ptr()), C.c_void_p(ys[off:].data_ptr()), prec)
             assert st == 0
             outs.append(ys[off:off + D].numpy().astype(np.float64).copy())
         for y in outs:
-            assert np.abs(y - yr).max() <= TOL32 * np.abs(yr).max()
-        assert np.abs(outs[0] - outs[1]).max() <= TOL32 * np.abs(yr).max()
+            assert np.abs(y - yr).max() <= tol * np.abs(yr).max()
+        assert np.abs(outs[0] - outs[1]).max() <= tol * np.abs(yr).max()
 
 
 def test_autotune_keeps_parity(synth, dg):
