@@ -41,8 +41,9 @@ namespace {
 constexpr int kPairThreads = 256;
 constexpr int kPairWarps = kPairThreads / 32;
 constexpr uint32_t kNone = 0xffffffffu;
-// tile[q][s] (orbital-major): mma fragment loads (bank 8t + g) and the
-// same-orbital writes of a warp's 32 sets are free of bank conflicts
+// tile[q][s] (orbital-major): mma fragment loads (bank 8t + g), the result
+// stores (output slots permuted, see the K fragments) and the same-orbital
+// writes of a warp's 32 sets are free of bank conflicts
 constexpr int kTileStride = 40;
 
 struct PairShape {
@@ -126,7 +127,10 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
     __syncthreads();
     for (int e = threadIdx.x; e < 4 * 4 * 32; e += blockDim.x) {
       const int kt = e >> 7, nt = (e >> 5) & 3, ln = e & 31;
-      const int a0 = 8 * kt + (ln & 3), a1 = a0 + 4, i = 8 * nt + (ln >> 2);
+      // product column j of n tile nt is output slot 8 nt + (j >> 1) + 4 (j & 1):
+      // a lane's two result columns 2t, 2t + 1 land in slot rows t and t + 4,
+      // which keeps the result stores free of bank conflicts
+      const int a0 = 8 * kt + (ln & 3), a1 = a0 + 4, j = ln >> 2, i = 8 * nt + (j >> 1) + 4 * (j & 1);
       auto orb = [&](int col) { return col < sp ? col : col < keff ? sm.hole_o[col - sp] : -1; };
       const int o0 = orb(a0), o1 = orb(a1), oi = orb(i);
       const bool v0 = o0 >= 0 && oi >= 0, v1 = o1 >= 0 && oi >= 0;
@@ -206,11 +210,11 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
 #pragma unroll
           for (int nt = 0; nt < 4; ++nt)
             if (nt < nk) {
-              const int q0 = 8 * nt + 2 * tq;
+              const int q0 = 8 * nt + tq;  // columns 2t, 2t + 1 are slots t, t + 4
               tile[q0][r0] = cc[nt][0];
-              tile[q0 + 1][r0] = cc[nt][1];
+              tile[q0 + 4][r0] = cc[nt][1];
               tile[q0][r0 + 8] = cc[nt][2];
-              tile[q0 + 1][r0 + 8] = cc[nt][3];
+              tile[q0 + 4][r0 + 8] = cc[nt][3];
             }
         }
       }
