@@ -41,9 +41,12 @@ namespace {
 constexpr int kPairThreads = 256;
 constexpr int kPairWarps = kPairThreads / 32;
 constexpr uint32_t kNone = 0xffffffffu;
-// tile[q][s] (orbital-major): mma fragment loads (bank 8t + g), the result
-// stores (output slots permuted, see the K fragments) and the same-orbital
-// writes of a warp's 32 sets are free of bank conflicts
+// tile[q][c] (orbital-major; set s of the warp's 32 at column
+// c = 16 (s >> 4) + 2 (s & 7) + ((s >> 3) & 1), so the sets g and g + 8 of an
+// m-tile, which one mma lane holds, are neighbours): the 8-byte mma fragment
+// loads (bank 8t + 2g), the 8-byte result stores (output slots permuted, see
+// the K fragments) and the same-orbital writes of a warp's 32 sets are free
+// of bank conflicts
 constexpr int kTileStride = 40;
 
 struct PairShape {
@@ -103,6 +106,7 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, tq = lane & 3;
   float(*tile)[kTileStride] = sm.tile[warp];
+  const int pc = 16 * (lane >> 4) + 2 * (lane & 7) + ((lane >> 3) & 1);  // this lane's set column
   {
     float4 *tz = reinterpret_cast<float4 *>(&tile[0][0]);
     for (int z = lane; z < 32 * kTileStride / 4; z += 32) tz[z] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -168,14 +172,14 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
         for (int h = 0; h < 16; ++h)
           if (h < nch) {
             const uint32_t e = lane_of(ent[h >> 2], h & 3);
-            tile[e & 0xffu][lane] = __ldg(x + own + (e >> 8));
+            tile[e & 0xffu][pc] = __ldg(x + own + (e >> 8));
           }
-        for (int h = 0; h < nhr; ++h) tile[sp + h][lane] = __ldg(x + sm.hole_rs[h] + c);
+        for (int h = 0; h < nhr; ++h) tile[sp + h][pc] = __ldg(x + sm.hole_rs[h] + c);
       }
       __syncwarp();
       // Y = X K on the tensor cores: 3xTF32 (lo*hi + hi*lo + hi*hi)
       {
-        // one m-tile (16 sets) at a time: its rows of the tile are disjoint
+        // one m-tile (16 sets) at a time: its columns of the tile are disjoint
         // from the other m-tile's, so its Y may overwrite its X at once
 #pragma unroll
         for (int mt = 0; mt < 2; ++mt) {
@@ -184,13 +188,15 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
           for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
             for (int e = 0; e < 4; ++e) cc[nt][e] = 0.f;
-          const int r0 = 16 * mt + g;
+          const int r0 = 16 * mt + 2 * g;  // columns of the sets 16 mt + g and 16 mt + g + 8
 #pragma unroll
           for (int kt = 0; kt < 4; ++kt) {
             if (kt < nk) {
               uint32_t ah[4], al[4];
               const int k0 = 8 * kt + tq;
-              const float f[4] = {tile[k0][r0], tile[k0][r0 + 8], tile[k0 + 4][r0], tile[k0 + 4][r0 + 8]};
+              const float2 p0 = *reinterpret_cast<const float2 *>(&tile[k0][r0]);
+              const float2 p1 = *reinterpret_cast<const float2 *>(&tile[k0 + 4][r0]);
+              const float f[4] = {p0.x, p0.y, p1.x, p1.y};
 #pragma unroll
               for (int e = 0; e < 4; ++e) {
                 ah[e] = to_tf32(f[e]);
@@ -211,10 +217,8 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
           for (int nt = 0; nt < 4; ++nt)
             if (nt < nk) {
               const int q0 = 8 * nt + tq;  // columns 2t, 2t + 1 are slots t, t + 4
-              tile[q0][r0] = cc[nt][0];
-              tile[q0 + 4][r0] = cc[nt][1];
-              tile[q0][r0 + 8] = cc[nt][2];
-              tile[q0 + 4][r0 + 8] = cc[nt][3];
+              *reinterpret_cast<float2 *>(&tile[q0][r0]) = make_float2(cc[nt][0], cc[nt][2]);
+              *reinterpret_cast<float2 *>(&tile[q0 + 4][r0]) = make_float2(cc[nt][1], cc[nt][3]);
             }
         }
       }
@@ -231,9 +235,9 @@ sigma_pair_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32_t 
         for (int h = 0; h < 16; ++h)
           if (h < nch) {
             const uint32_t e = lane_of(ent[h >> 2], h & 3);
-            atomicAdd(y + own + (e >> 8), tile[e & 0xffu][lane]);
+            atomicAdd(y + own + (e >> 8), tile[e & 0xffu][pc]);
           }
-        for (int h = 0; h < nhr; ++h) atomicAdd(y + sm.hole_rs[h] + c, tile[sp + h][lane]);
+        for (int h = 0; h < nhr; ++h) atomicAdd(y + sm.hole_rs[h] + c, tile[sp + h][pc]);
       }
       __syncwarp();  // the tile is cleared by the next round
     }
