@@ -315,8 +315,8 @@ sigma_pair_ff_kernel(PairShape s, const uint2 *__restrict__ blocks, const uint32
           const ff *Krow = Kc + slot[to] * 32;
           ff acc(0);
 #pragma unroll
-          for (int ti = 0; ti < NO; ++ti)
-            if (ti < nopen) acc += Krow[slot[ti]] * X[ti];
+          for (int ti = 0; ti < NO; ++ti)  // K_ii = 0: the diagonal term is skipped (same sum, bit for bit)
+            if (ti < nopen && ti != to) acc += Krow[slot[ti]] * X[ti];
           atomicAdd(y + tgt[to], ff_to(acc));
         }
       }
