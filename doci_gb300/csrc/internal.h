@@ -107,7 +107,7 @@ struct doci_ham {
   // once the last piece its rows reach is up, and a piece of sigma goes down
   // once the last group touching it is done.  d_pblocks_host holds the units
   // in group order, largest first within a group.
-  static constexpr int kHostChunks = 8;
+  static constexpr int kHostChunks = 16;
   struct HostGroup {
     int first, count;          // units [first, first + count) of d_pblocks_host
     int need;                  // last upload piece its rows reach

@@ -366,7 +366,8 @@ struct HostUnit {
 // every group reaching it is done.  The order minimises the modelled end of
 // the download: GB300 measurements, upload 211 GB/s, download 193 GB/s, the
 // pair kernel 0.061 ns per set; a deterministic local search (random pair
-// swaps from the order by last piece) over the at most 36 groups.  The model
+// swaps from the order by last piece) over the groups (at most
+// kHostChunks (kHostChunks + 1) / 2).  The model
 // only orders the work: every order gives the same sigma.
 void host_schedule(doci_ham *h, const std::vector<HostUnit> &hu, std::vector<uint32_t> &flat) {
   constexpr int NC = doci_ham::kHostChunks;
