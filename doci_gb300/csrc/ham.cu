@@ -76,11 +76,14 @@ void ham_release(doci_ham *h) {
     cudaStreamSynchronize(st);
     cudaStreamDestroy(st);
   }
-  if (h->copy_stream) {
-    cudaStreamSynchronize(h->copy_stream);
-    cudaStreamDestroy(h->copy_stream);
+  for (cudaStream_t *s : {&h->copy_stream, &h->side_stream}) {
+    if (*s) {
+      cudaStreamSynchronize(*s);
+      cudaStreamDestroy(*s);
+    }
+    *s = nullptr;
   }
-  for (cudaEvent_t *e : {&h->start_ev, &h->end_ev}) {
+  for (cudaEvent_t *e : {&h->start_ev, &h->end_ev, &h->side_ev}) {
     if (*e) cudaEventDestroy(*e);
     *e = nullptr;
   }
@@ -88,11 +91,13 @@ void ham_release(doci_ham *h) {
     if (e) cudaEventDestroy(e);
     e = nullptr;
   }
-  for (auto &e : h->down_ev) {
+  for (auto &e : h->init_ev) {
     if (e) cudaEventDestroy(e);
     e = nullptr;
   }
-  h->copy_stream = nullptr;
+  for (auto &e : h->group_ev)
+    if (e) cudaEventDestroy(e);
+  h->group_ev.clear();
   h->d_pblocks_host = nullptr;
   h->host_groups.clear();
   h->d_binom = nullptr;

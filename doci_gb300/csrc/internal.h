@@ -101,24 +101,28 @@ struct doci_ham {
   uint32_t *d_pblocks = nullptr;
   int npblocks = 0;
   void *d_kfrag = nullptr;
-  // doci_sigma_host on the FP32 pair form: x and sigma cross the host link
-  // in kHostChunks contiguous pieces (chunk_off) on copy_stream while the
-  // pair units run in groups (sigma_pair.cu, host_schedule): a group starts
-  // once the last piece its rows reach is up, and a piece of sigma goes down
-  // once the last group touching it is done.  d_pblocks_host holds the units
-  // in group order, largest first within a group.
+  // doci_sigma_host on the pair forms: x and sigma cross the host link in
+  // kHostChunks contiguous pieces (chunk_off) on copy_stream while the pair
+  // units run in groups (sigma_pair.cu, host_schedule), alternately on the
+  // handle's stream and side_stream: a group starts once the last piece its
+  // rows reach is up, and a piece of sigma goes down once every group
+  // touching it is done.  d_pblocks_host holds the units in group order,
+  // largest first within a group.
   static constexpr int kHostChunks = 16;
   struct HostGroup {
     int first, count;          // units [first, first + count) of d_pblocks_host
     int need;                  // last upload piece its rows reach
+    uint32_t touch_mask;       // pieces its rows reach
     uint32_t init_mask;        // pieces whose sigma = diag * x pass runs first
     uint32_t down_mask;        // pieces final after it
   };
   uint32_t *d_pblocks_host = nullptr;
   std::vector<HostGroup> host_groups;
   uint64_t chunk_off[kHostChunks + 1] = {};
-  cudaStream_t copy_stream = nullptr;
-  cudaEvent_t up_ev[kHostChunks] = {}, down_ev[kHostChunks] = {}, start_ev = nullptr, end_ev = nullptr;
+  cudaStream_t copy_stream = nullptr, side_stream = nullptr;
+  cudaEvent_t up_ev[kHostChunks] = {}, init_ev[kHostChunks] = {}, start_ev = nullptr, end_ev = nullptr,
+              side_ev = nullptr;
+  std::vector<cudaEvent_t> group_ev;  // one per host group
 
   // error word of the tensor-core sigma's bounded waits (0 = none)
   int *d_tc_err = nullptr;

@@ -448,6 +448,7 @@ void host_schedule(doci_ham *h, const std::vector<HostUnit> &hu, std::vector<uin
     }
     hg.count = static_cast<int>(c.units.size());
     hg.need = c.last;
+    hg.touch_mask = c.mask;
     const uint32_t upto = (c.last + 1 >= 32) ? 0xffffffffu : ((1u << (c.last + 1)) - 1u);
     hg.init_mask = upto & ~inited;
     inited |= hg.init_mask;
@@ -460,6 +461,7 @@ void host_schedule(doci_ham *h, const std::vector<HostUnit> &hu, std::vector<uin
   tail.first = static_cast<int>(flat.size() / 2);
   tail.count = 0;
   tail.need = NC - 1;
+  tail.touch_mask = 0;
   tail.init_mask = ((1u << NC) - 1u) & ~inited;
   for (int k = 0; k < NC; ++k)
     if (last_of[k] < 0) tail.down_mask |= 1u << k;
@@ -560,57 +562,94 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
 namespace {
 
 // One host-buffer sigma on the group schedule of host_schedule: the pieces
-// of hx go up in order on the copy stream; on st, per group, init(a, n) runs
-// the diagonal pass of each piece the group is the first to reach and
-// group(first, count) its units; with hy, each piece of dy goes down (copy
-// stream) once no later group reaches it, and st waits for the last one.
+// of hx go up in order on the copy stream; the groups run alternately on st
+// and the side stream (the sums are atomic adds, so groups may overlap; a
+// group's launch tail then overlaps the next group's start), each after its
+// last piece is up: init(a, n) runs the diagonal pass of each piece a group
+// is the first to reach (on that group's stream; groups on the other stream
+// that reach the piece wait for it), group(first, count, stream) its units;
+// with hy, each piece of dy goes down (copy stream) once every group reaching
+// it is done.  st waits for the side stream and the downloads at the end.
 template <typename T, typename Init, typename Group>
 int run_host_schedule(doci_ham *h, const T *hx, T *dx, T *dy, T *hy, cudaStream_t st, Init init, Group group) {
   constexpr int NC = doci_ham::kHostChunks;
+  const int ng = static_cast<int>(h->host_groups.size());
   if (!h->copy_stream) {
     DOCI_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    DOCI_CUDA(cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking));
     for (auto &e : h->up_ev) DOCI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    for (auto &e : h->down_ev) DOCI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &e : h->init_ev) DOCI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     DOCI_CUDA(cudaEventCreateWithFlags(&h->start_ev, cudaEventDisableTiming));
     DOCI_CUDA(cudaEventCreateWithFlags(&h->end_ev, cudaEventDisableTiming));
+    DOCI_CUDA(cudaEventCreateWithFlags(&h->side_ev, cudaEventDisableTiming));
+  }
+  while (static_cast<int>(h->group_ev.size()) < ng) {
+    cudaEvent_t e = nullptr;
+    DOCI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->group_ev.push_back(e);
   }
   cudaStream_t cs = h->copy_stream;
-  // the upload starts after the stream's earlier work (dx may still be read)
+  cudaStream_t run[2] = {st, h->side_stream};
+  // everything starts after the stream's earlier work (dx may still be read)
   DOCI_CUDA(cudaEventRecord(h->start_ev, st));
   DOCI_CUDA(cudaStreamWaitEvent(cs, h->start_ev, 0));
+  DOCI_CUDA(cudaStreamWaitEvent(run[1], h->start_ev, 0));
   for (int k = 0; k < NC; ++k) {
     const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
     if (n) DOCI_CUDA(cudaMemcpyAsync(dx + a, hx + a, n * sizeof(T), cudaMemcpyHostToDevice, cs));
     DOCI_CUDA(cudaEventRecord(h->up_ev[k], cs));
   }
-  int waited = -1;
-  for (const doci_ham::HostGroup &g : h->host_groups) {
-    if (g.need > waited) {  // pieces go up in order: waiting for the last one covers the rest
-      DOCI_CUDA(cudaStreamWaitEvent(st, h->up_ev[g.need], 0));
-      waited = g.need;
+  int waited[2] = {-1, -1};
+  int init_on[NC];        // stream that ran the piece's diagonal pass
+  int last_touch[2][NC];  // per stream: last group reaching the piece
+  for (int k = 0; k < NC; ++k) {
+    init_on[k] = -1;
+    last_touch[0][k] = last_touch[1][k] = -1;
+  }
+  for (int gi = 0; gi < ng; ++gi) {
+    const doci_ham::HostGroup &g = h->host_groups[gi];
+    const int r = gi & 1;
+    cudaStream_t s = run[r];
+    if (g.need > waited[r]) {  // pieces go up in order: waiting for the last one covers the rest
+      DOCI_CUDA(cudaStreamWaitEvent(s, h->up_ev[g.need], 0));
+      waited[r] = g.need;
     }
     for (int k = 0; k < NC; ++k) {
       if (!(g.init_mask >> k & 1u)) continue;
       const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
       if (n) {
-        const int r = init(a, n);
-        if (r != DOCI_OK) return r;
+        const int rc = init(a, n, s);
+        if (rc != DOCI_OK) return rc;
       }
+      DOCI_CUDA(cudaEventRecord(h->init_ev[k], s));
+      init_on[k] = r;
     }
+    for (int k = 0; k < NC; ++k)
+      if ((g.touch_mask >> k & 1u) && init_on[k] == 1 - r) {
+        DOCI_CUDA(cudaStreamWaitEvent(s, h->init_ev[k], 0));
+        init_on[k] = 2;  // both streams are ordered after it now
+      }
     if (g.count > 0) {
-      const int r = group(g.first, g.count);
-      if (r != DOCI_OK) return r;
+      const int rc = group(g.first, g.count, s);
+      if (rc != DOCI_OK) return rc;
     }
+    DOCI_CUDA(cudaEventRecord(h->group_ev[gi], s));
+    for (int k = 0; k < NC; ++k)
+      if (g.touch_mask >> k & 1u) last_touch[r][k] = gi;
     if (!hy) continue;
     // pieces no later group reaches go down now, behind the upload
     for (int k = 0; k < NC; ++k) {
       if (!(g.down_mask >> k & 1u)) continue;
       const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
-      DOCI_CUDA(cudaEventRecord(h->down_ev[k], st));
-      DOCI_CUDA(cudaStreamWaitEvent(cs, h->down_ev[k], 0));
+      DOCI_CUDA(cudaStreamWaitEvent(cs, h->group_ev[gi], 0));
+      const int other = last_touch[1 - r][k];
+      if (other >= 0) DOCI_CUDA(cudaStreamWaitEvent(cs, h->group_ev[other], 0));
+      if (init_on[k] == 1 - r) DOCI_CUDA(cudaStreamWaitEvent(cs, h->init_ev[k], 0));
       if (n) DOCI_CUDA(cudaMemcpyAsync(hy + a, dy + a, n * sizeof(T), cudaMemcpyDeviceToHost, cs));
     }
   }
+  DOCI_CUDA(cudaEventRecord(h->side_ev, run[1]));
+  DOCI_CUDA(cudaStreamWaitEvent(st, h->side_ev, 0));
   if (hy) {
     DOCI_CUDA(cudaEventRecord(h->end_ev, cs));
     DOCI_CUDA(cudaStreamWaitEvent(st, h->end_ev, 0));
@@ -634,16 +673,16 @@ int launch_pair_ff_host_no(doci_ham *h, const double *hx, double *dx, double *dy
   const uint2 *blocks = reinterpret_cast<const uint2 *>(h->d_pblocks_host);
   r = run_host_schedule<double>(
       h, hx, dx, dy, hy, st,
-      [&](uint64_t a, uint64_t n) {
-        pair_init64_kernel<<<init_grid(n), 256, 0, st>>>(static_cast<uint32_t>(n), h->d_diag + a, dx + a, dy + a,
-                                                          xf + a);
+      [&](uint64_t a, uint64_t n, cudaStream_t s) {
+        pair_init64_kernel<<<init_grid(n), 256, 0, s>>>(static_cast<uint32_t>(n), h->d_diag + a, dx + a, dy + a,
+                                                         xf + a);
         DOCI_CUDA(cudaGetLastError());
         return static_cast<int>(DOCI_OK);
       },
-      [&](int first, int count) {
-        const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, count};
-        sigma_pair_ff_kernel<NO><<<std::min(slots, count), kPairThreads, 0, st>>>(
-            s, blocks + first, h->d_rowstart, h->d_binom, h->d_Kmir64, h->d_ins_t, h->d_tab_off, xf, dy);
+      [&](int first, int count, cudaStream_t s) {
+        const PairShape ps{h->D, h->L, h->N, h->split, h->L - h->split, count};
+        sigma_pair_ff_kernel<NO><<<std::min(slots, count), kPairThreads, 0, s>>>(
+            ps, blocks + first, h->d_rowstart, h->d_binom, h->d_Kmir64, h->d_ins_t, h->d_tab_off, xf, dy);
         DOCI_CUDA(cudaGetLastError());
         return static_cast<int>(DOCI_OK);
       });
@@ -664,15 +703,15 @@ int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *
   const uint2 *blocks = reinterpret_cast<const uint2 *>(h->d_pblocks_host);
   return run_host_schedule<float>(
       h, hx, dx, dy, hy, st,
-      [&](uint64_t a, uint64_t n) {
-        pair_init_kernel<<<init_grid(n), 256, 0, st>>>(static_cast<uint32_t>(n), h->d_diag32 + a, dx + a, dy + a);
+      [&](uint64_t a, uint64_t n, cudaStream_t s) {
+        pair_init_kernel<<<init_grid(n), 256, 0, s>>>(static_cast<uint32_t>(n), h->d_diag32 + a, dx + a, dy + a);
         DOCI_CUDA(cudaGetLastError());
         return static_cast<int>(DOCI_OK);
       },
-      [&](int first, int count) {
-        const PairShape s{h->D, h->L, h->N, h->split, h->L - h->split, count};
-        sigma_pair_kernel<<<std::min(slots, count), kPairThreads, 0, st>>>(
-            s, blocks + first, h->d_rowstart, h->d_binom, reinterpret_cast<const float *>(h->d_kfrag), h->d_ins_t,
+      [&](int first, int count, cudaStream_t s) {
+        const PairShape ps{h->D, h->L, h->N, h->split, h->L - h->split, count};
+        sigma_pair_kernel<<<std::min(slots, count), kPairThreads, 0, s>>>(
+            ps, blocks + first, h->d_rowstart, h->d_binom, reinterpret_cast<const float *>(h->d_kfrag), h->d_ins_t,
             h->d_tab_off, dx, dy);
         DOCI_CUDA(cudaGetLastError());
         return static_cast<int>(DOCI_OK);
