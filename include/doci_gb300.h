@@ -215,7 +215,10 @@ int doci_sigma_plan(const doci_ham *ham, int precision, int *kind, int *launches
 /* Same on host buffers; copies in and out inside the call, synchronous.  On
  * the pair forms (kinds 6 and 9) x is uploaded, and a pinned (page-locked) y
  * downloaded, in pieces on the handle's own copy stream, overlapped with the
- * sigma. */
+ * sigma (whose unit groups alternate between the handle's stream and a
+ * second stream of its own).  The staging buffers and these streams belong
+ * to the handle: calls on one handle from several host threads must be
+ * serialised by the caller. */
 int doci_sigma_host(doci_ham *ham, const void *x, void *y, int precision);
 
 /* Lexical addressing on the device: bitstrings of determinants
