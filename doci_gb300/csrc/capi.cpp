@@ -506,6 +506,10 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
       op.x32 = static_cast<float *>(x32.p);
       op.y32 = static_cast<float *>(y32.p);
       a.shift = sv64.shift;  // the FP64 phase works on H - shift as well
+      // the FP32 corrections leave a noise floor in the run's residual: a run
+      // whose residual has not reached a new minimum for 25 iterations stops,
+      // and the next round re-anchors it from its vector with an FP64 sigma
+      a.stall_window = 25;
     }
     int its64 = 0;
     for (int round = 0;; ++round) {
@@ -530,7 +534,7 @@ int doci_solve_trace(doci_ham *h, const doci_solve_opts *opts, double *vec, doci
         r[2] = theta;
         r[3] = now_s() - trace_t0;
       }
-      if (out.converged || round >= 2 || res->iterations_fp32 + its64 >= o.max_its) break;
+      if (out.converged || round >= 3 || res->iterations_fp32 + its64 >= o.max_its) break;
       a.max_its = o.max_its - res->iterations_fp32 - its64;
       DOCI_CUDA(cudaMemcpyAsync(t.p, d_x, sizeof(double) * D, cudaMemcpyDeviceToDevice, st));
     }

@@ -250,9 +250,10 @@ int davidson_run(MatvecOp &op, size_t D, const double *d_diag, S *d_t, const Dav
       r[2] = theta + a.shift;
       r[3] = now_s() - a.trace_t0;
     }
-    // FP32 phase of the mixed mode: stop once the residual has not reached a
-    // new minimum for stall_window iterations (the FP32 noise floor; restarted
-    // Davidson residuals are not monotone, so a short window would stop early)
+    // mixed mode (FP32 phase, and the FP64 phase with FP32 corrections): stop
+    // once the residual has not reached a new minimum for stall_window
+    // iterations (the FP32 noise floor; restarted Davidson residuals are not
+    // monotone, so a short window would stop early)
     if (a.stall_window > 0) {
       if (res < best) {
         best = res;

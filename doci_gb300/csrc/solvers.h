@@ -45,7 +45,7 @@ struct DavidsonArgs {
   double tol = 1e-8;
   int print_table = 0;    // the -DDAVIDIT table of davidson.c:47-112
   int print_summary = 0;  // "** DAVIDSON ITERATIONS" (davidson.c:114)
-  int stall_window = 0;   // > 0: stop when the residual stops reaching new minima (FP32 phase)
+  int stall_window = 0;   // > 0: stop when the residual stops reaching new minima (mixed mode)
   // the operator is H - shift (energies are reported + shift; the
   // preconditioner's diagonal is the unshifted FP64 one)
   double shift = 0;
