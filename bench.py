@@ -217,15 +217,19 @@ def fp64_like_for_like(h, D, dg, torch, steps: int):
     hy = torch.empty(D, dtype=torch.float64).pin_memory()
     lib = dg.lib()
     assert lib.doci_sigma_host(h.handle, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()), dg.FP64) == 0
+    calls = []
     t0 = time.perf_counter()
     for _ in range(steps):
+        tc = time.perf_counter()
         assert lib.doci_sigma_host(h.handle, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()), dg.FP64) == 0
+        calls.append(time.perf_counter() - tc)
     te = (time.perf_counter() - t0) / steps
     return {"value": round(D / ms / 1e6, 4), "unit": UNIT, "sigma_ms": round(ms, 3),
             "sigma_kernel": KERNEL_NAMES.get(kind, kind), "dtype": "f64 (float-float pair form)" if kind == 9 else "f64",
             "e2e": {"value": round(D / te / 1e9, 4), "unit": UNIT, "ms_per_call": round(te * 1e3, 3),
                     "h2d_bytes_per_step": D * 8, "d2h_bytes_per_step": D * 8,
-                    "call": "doci_sigma_host FP64 (C ABI, pinned host buffers)", "steps": steps}}
+                    "call": "doci_sigma_host FP64 (C ABI, pinned host buffers)", "steps": steps,
+                    "per_call_ms": [round(c * 1e3, 2) for c in calls]}}
 
 
 def converge_report(h, max_vec: int, mixed_tol: float, threshold: float = 1e-8):
@@ -634,14 +638,18 @@ def main():
         assert st == 0, st
         if ws > 1:
             dist.barrier()
+        calls = []
         t0 = time.perf_counter()
         for _ in range(a.e2e_steps):
+            tc = time.perf_counter()
             st = lib.doci_sigma_host(h.handle, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()), prec)
+            calls.append(time.perf_counter() - tc)
             assert st == 0, st
         te = max_over_ranks(time.perf_counter() - t0, ws)
         e2e = {"value": round(replica_gdets(D, a.e2e_steps, ws, te), 4), "unit": UNIT,
                "h2d_bytes_per_step": D * esize, "d2h_bytes_per_step": D * esize,
-               "call": "doci_sigma_host (C ABI, pinned host buffers)", "steps": a.e2e_steps}
+               "call": "doci_sigma_host (C ABI, pinned host buffers)", "steps": a.e2e_steps,
+               "per_call_ms": [round(c * 1e3, 2) for c in calls]}
     fp64 = None
     if prec == dg.FP32 and nv == 1 and not a.no_fp64 and rank == 0:
         fp64 = fp64_like_for_like(h, D, dg, torch, a.e2e_steps)
