@@ -297,7 +297,7 @@ int doci_sigma_host(doci_ham *h, const void *x, void *y, int precision) {
   const void *dx = words ? mapped_host(x) : nullptr;
   void *dy = words ? const_cast<void *>(mapped_host(y)) : nullptr;
   const int kind = plan_sigma(h, precision).kind;
-  const bool sched = h->d_pblocks_host && !h->host_groups.empty();
+  const bool sched = h->d_pblocks_host && !h->host_steps.empty();
   if (sched && ((precision == DOCI_FP32 && kind == 6 && pair_fits(h)) ||
                 (precision == DOCI_FP64 && kind == 9 && pair_ff_fits(h)))) {
     // the pair forms overlap the copies with the sigma: pieces of x go up and

@@ -100,6 +100,7 @@ void ham_release(doci_ham *h) {
   h->group_ev.clear();
   h->d_pblocks_host = nullptr;
   h->host_groups.clear();
+  h->host_steps.clear();
   h->d_binom = nullptr;
   h->d_Kmir64 = h->d_tab64 = h->d_diag = nullptr;
   h->d_Kmir32 = h->d_diag32 = nullptr;

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/doci_gb300.h"
+#include "host_plan.h"
 
 namespace doci {
 
@@ -102,22 +103,14 @@ struct doci_ham {
   int npblocks = 0;
   void *d_kfrag = nullptr;
   // doci_sigma_host on the pair forms: x and sigma cross the host link in
-  // kHostChunks contiguous pieces (chunk_off) on copy_stream while the pair
-  // units run in groups (sigma_pair.cu, host_schedule), alternately on the
-  // handle's stream and side_stream: a group starts once the last piece its
-  // rows reach is up, and a piece of sigma goes down once every group
-  // touching it is done.  d_pblocks_host holds the units in group order,
-  // largest first within a group.
-  static constexpr int kHostChunks = 16;
-  struct HostGroup {
-    int first, count;          // units [first, first + count) of d_pblocks_host
-    int need;                  // last upload piece its rows reach
-    uint32_t touch_mask;       // pieces its rows reach
-    uint32_t init_mask;        // pieces whose sigma = diag * x pass runs first
-    uint32_t down_mask;        // pieces final after it
-  };
+  // pieces (chunk_off) on copy_stream while the pair units run in groups,
+  // alternately on the handle's stream and side_stream (host_plan.h):
+  // d_pblocks_host holds the units in group order, host_steps what each
+  // group's launch waits for and which pieces go down after it.
+  static constexpr int kHostChunks = doci::hostplan::kPieces;
   uint32_t *d_pblocks_host = nullptr;
-  std::vector<HostGroup> host_groups;
+  std::vector<doci::hostplan::Group> host_groups;
+  std::vector<doci::hostplan::Step> host_steps;
   uint64_t chunk_off[kHostChunks + 1] = {};
   cudaStream_t copy_stream = nullptr, side_stream = nullptr;
   cudaEvent_t up_ev[kHostChunks] = {}, init_ev[kHostChunks] = {}, start_ev = nullptr, end_ev = nullptr,

@@ -27,8 +27,6 @@
 
 #include <algorithm>
 #include <cstring>
-#include <map>
-#include <random>
 #include <vector>
 
 #include "addressing.cuh"
@@ -352,124 +350,6 @@ bool pair_fits(const doci_ham *h) {
   return static_cast<size_t>(h->max_row) * sizeof(float) <= 100 * 1024;
 }
 
-namespace {
-
-struct HostUnit {
-  uint32_t own, word;  // as in d_pblocks
-  uint64_t sets;       // (N-1)-pair sets of the unit
-  uint32_t touched;    // pieces its rows reach
-};
-
-// Order of the unit groups for the host-buffer sigma.  Units are grouped by
-// (first, last) piece their rows reach; a group can start once its last
-// piece is up (pieces go up in order), and a piece of sigma can go down once
-// every group reaching it is done.  The order minimises the modelled end of
-// the download: GB300 measurements, upload 211 GB/s, download 193 GB/s, the
-// pair kernel 0.061 ns per set; a deterministic local search (random pair
-// swaps from the order by last piece) over the groups (at most
-// kHostChunks (kHostChunks + 1) / 2).  The model
-// only orders the work: every order gives the same sigma.
-void host_schedule(doci_ham *h, const std::vector<HostUnit> &hu, std::vector<uint32_t> &flat) {
-  constexpr int NC = doci_ham::kHostChunks;
-  struct Cls {
-    double sets = 0;
-    int first = NC, last = -1;
-    uint32_t mask = 0;
-    std::vector<const HostUnit *> units;
-  };
-  std::map<std::pair<int, int>, Cls> by;
-  for (const HostUnit &u : hu) {
-    if (!u.touched) continue;
-    const int lo = __builtin_ctz(u.touched), hi = 31 - __builtin_clz(u.touched);
-    Cls &c = by[{lo, hi}];
-    c.sets += static_cast<double>(u.sets);
-    c.first = lo;
-    c.last = hi;
-    c.mask |= u.touched;
-    c.units.push_back(&u);
-  }
-  std::vector<Cls> cls;
-  for (auto &kv : by) cls.push_back(std::move(kv.second));
-  double total = 0;
-  for (auto &c : cls) total += c.sets;
-  const double piece_bytes = static_cast<double>(h->D) * sizeof(float) / NC;
-  const double t_up = piece_bytes / 211e9, t_down = piece_bytes / 193e9, t_set = 0.061e-9;
-  auto model = [&](const std::vector<int> &order) {
-    double t = 0, ready[NC];
-    for (double &r : ready) r = -1;
-    for (int i : order) {
-      const Cls &c = cls[i];
-      t = std::max(t, (c.last + 1) * t_up) + c.sets * t_set;
-      for (int k = 0; k < NC; ++k)
-        if (c.mask >> k & 1u) ready[k] = t;
-    }
-    t = std::max(t, NC * t_up);
-    for (double &r : ready)
-      if (r < 0) r = t;
-    std::sort(ready, ready + NC);
-    double d = 0;
-    for (double r : ready) d = std::max(d, r) + t_down;
-    return d;
-  };
-  std::vector<int> order(cls.size());
-  for (size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int>(i);
-  std::sort(order.begin(), order.end(), [&](int a, int b) {
-    return cls[a].last != cls[b].last ? cls[a].last < cls[b].last : cls[a].first < cls[b].first;
-  });
-  double best = model(order);
-  if (order.size() > 1) {
-    std::mt19937 rng(12345);
-    std::uniform_int_distribution<size_t> pick(0, order.size() - 1);
-    for (int it = 0; it < 20000; ++it) {
-      std::vector<int> o = order;
-      std::swap(o[pick(rng)], o[pick(rng)]);
-      const double v = model(o);
-      if (v <= best) {
-        best = v;
-        order.swap(o);
-      }
-    }
-  }
-  h->host_groups.clear();
-  flat.clear();
-  uint32_t inited = 0;
-  int last_of[NC];
-  for (int &l : last_of) l = -1;
-  for (size_t g = 0; g < order.size(); ++g)
-    for (int k = 0; k < NC; ++k)
-      if (cls[order[g]].mask >> k & 1u) last_of[k] = static_cast<int>(g);
-  for (size_t g = 0; g < order.size(); ++g) {
-    const Cls &c = cls[order[g]];
-    doci_ham::HostGroup hg{};
-    hg.first = static_cast<int>(flat.size() / 2);
-    for (const HostUnit *u : c.units) {
-      flat.push_back(u->own);
-      flat.push_back(u->word);
-    }
-    hg.count = static_cast<int>(c.units.size());
-    hg.need = c.last;
-    hg.touch_mask = c.mask;
-    const uint32_t upto = (c.last + 1 >= 32) ? 0xffffffffu : ((1u << (c.last + 1)) - 1u);
-    hg.init_mask = upto & ~inited;
-    inited |= hg.init_mask;
-    for (int k = 0; k < NC; ++k)
-      if (last_of[k] == static_cast<int>(g)) hg.down_mask |= 1u << k;
-    h->host_groups.push_back(hg);
-  }
-  // pieces no unit reaches: their diagonal pass and download close the call
-  doci_ham::HostGroup tail{};
-  tail.first = static_cast<int>(flat.size() / 2);
-  tail.count = 0;
-  tail.need = NC - 1;
-  tail.touch_mask = 0;
-  tail.init_mask = ((1u << NC) - 1u) & ~inited;
-  for (int k = 0; k < NC; ++k)
-    if (last_of[k] < 0) tail.down_mask |= 1u << k;
-  if (tail.init_mask || tail.down_mask) h->host_groups.push_back(tail);
-}
-
-}  // namespace
-
 int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
   const int L = h->L, N = h->N, sp = h->split, na = L - sp;
   // K (mirrored orbitals, zero outside 0..L-1) split into TF32 high and low
@@ -498,30 +378,23 @@ int ham_build_pairs(doci_ham *h, const std::vector<uint32_t> &start) {
     flat.push_back(e.second.second);
   }
   h->npblocks = static_cast<int>(bl.size());
-  // host-buffer path: pieces of the vector and the group schedule
-  constexpr int NC = doci_ham::kHostChunks;
-  for (int k = 0; k <= NC; ++k) h->chunk_off[k] = static_cast<uint64_t>(h->D) * k / NC;
-  auto chunk_of = [&](uint64_t t) {
-    int k = 0;
-    while (k + 1 < NC && h->chunk_off[k + 1] <= t) ++k;
-    return k;
-  };
-  std::vector<HostUnit> hu;
+  // host-buffer path: pieces of the vector, units by the pieces their rows
+  // reach, the group schedule and its launch steps (host_plan.h)
+  hostplan::pieces(h->D, h->chunk_off);
+  std::vector<hostplan::Unit> hu;
   hu.reserve(bl.size());
   for (auto &e : bl) {
     const uint32_t mask = e.second.second & 0xffffffu;
     const int kp = static_cast<int>(e.second.second >> 24), jp = N - 1 - kp;
     uint32_t touched = 0;
-    auto row = [&](uint64_t rs, uint64_t len) {
-      for (int c = chunk_of(rs); c <= chunk_of(rs + len - 1); ++c) touched |= 1u << c;
-    };
-    if (e.second.first != kNone) row(e.second.first, binom64(sp, jp + 1));
+    if (e.second.first != kNone) touched |= hostplan::row_pieces(h->chunk_off, e.second.first, binom64(sp, jp + 1));
     for (int b = 0; b < na; ++b)
-      if (!(mask >> b & 1u)) row(start[mask | (1u << b)], binom64(sp, jp));
+      if (!(mask >> b & 1u)) touched |= hostplan::row_pieces(h->chunk_off, start[mask | (1u << b)], binom64(sp, jp));
     hu.push_back({e.second.first, e.second.second, binom64(sp, jp), touched});
   }
   std::vector<uint32_t> flat_host;
-  host_schedule(h, hu, flat_host);
+  hostplan::schedule(hu, h->D, h->host_groups, flat_host);
+  h->host_steps = hostplan::steps(h->host_groups);
   DOCI_CUDA(cudaMallocAsync(&h->d_kfrag, ks.size() * sizeof(float), h->stream));
   DOCI_CUDA(cudaMemcpyAsync(h->d_kfrag, ks.data(), ks.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   if (!flat.empty()) {
@@ -561,19 +434,18 @@ int launch_pair(const doci_ham *h, const float *x, float *y, cudaStream_t st) {
 
 namespace {
 
-// One host-buffer sigma on the group schedule of host_schedule: the pieces
-// of hx go up in order on the copy stream; the groups run alternately on st
-// and the side stream (the sums are atomic adds, so groups may overlap; a
-// group's launch tail then overlaps the next group's start), each after its
-// last piece is up: init(a, n) runs the diagonal pass of each piece a group
-// is the first to reach (on that group's stream; groups on the other stream
-// that reach the piece wait for it), group(first, count, stream) its units;
-// with hy, each piece of dy goes down (copy stream) once every group reaching
-// it is done.  st waits for the side stream and the downloads at the end.
+// One host-buffer sigma on the plan of host_plan.h (h->host_steps): the
+// pieces of hx go up in order on the copy stream; per step, on its compute
+// stream (the handle's stream st or the side stream), the wait for its last
+// piece, init(a, n, stream) for the diagonal passes it runs first (each
+// followed by the piece's init event), the waits for diagonal passes run on
+// the other stream, group(first, count, stream) for its units and the
+// group's event; with hy, the pieces final after the step go down on the
+// copy stream.  st waits for the side stream and the downloads at the end.
 template <typename T, typename Init, typename Group>
 int run_host_schedule(doci_ham *h, const T *hx, T *dx, T *dy, T *hy, cudaStream_t st, Init init, Group group) {
   constexpr int NC = doci_ham::kHostChunks;
-  const int ng = static_cast<int>(h->host_groups.size());
+  const int ng = static_cast<int>(h->host_steps.size());
   if (!h->copy_stream) {
     DOCI_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
     DOCI_CUDA(cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking));
@@ -599,52 +471,33 @@ int run_host_schedule(doci_ham *h, const T *hx, T *dx, T *dy, T *hy, cudaStream_
     if (n) DOCI_CUDA(cudaMemcpyAsync(dx + a, hx + a, n * sizeof(T), cudaMemcpyHostToDevice, cs));
     DOCI_CUDA(cudaEventRecord(h->up_ev[k], cs));
   }
-  int waited[2] = {-1, -1};
-  int init_on[NC];        // stream that ran the piece's diagonal pass
-  int last_touch[2][NC];  // per stream: last group reaching the piece
-  for (int k = 0; k < NC; ++k) {
-    init_on[k] = -1;
-    last_touch[0][k] = last_touch[1][k] = -1;
-  }
   for (int gi = 0; gi < ng; ++gi) {
-    const doci_ham::HostGroup &g = h->host_groups[gi];
-    const int r = gi & 1;
-    cudaStream_t s = run[r];
-    if (g.need > waited[r]) {  // pieces go up in order: waiting for the last one covers the rest
-      DOCI_CUDA(cudaStreamWaitEvent(s, h->up_ev[g.need], 0));
-      waited[r] = g.need;
-    }
+    const hostplan::Step &p = h->host_steps[gi];
+    const hostplan::Group &g = h->host_groups[gi];
+    cudaStream_t s = run[p.stream];
+    if (p.wait_up >= 0) DOCI_CUDA(cudaStreamWaitEvent(s, h->up_ev[p.wait_up], 0));
     for (int k = 0; k < NC; ++k) {
-      if (!(g.init_mask >> k & 1u)) continue;
+      if (!(p.init >> k & 1u)) continue;
       const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
       if (n) {
         const int rc = init(a, n, s);
         if (rc != DOCI_OK) return rc;
       }
       DOCI_CUDA(cudaEventRecord(h->init_ev[k], s));
-      init_on[k] = r;
     }
     for (int k = 0; k < NC; ++k)
-      if ((g.touch_mask >> k & 1u) && init_on[k] == 1 - r) {
-        DOCI_CUDA(cudaStreamWaitEvent(s, h->init_ev[k], 0));
-        init_on[k] = 2;  // both streams are ordered after it now
-      }
+      if (p.wait_init >> k & 1u) DOCI_CUDA(cudaStreamWaitEvent(s, h->init_ev[k], 0));
     if (g.count > 0) {
       const int rc = group(g.first, g.count, s);
       if (rc != DOCI_OK) return rc;
     }
     DOCI_CUDA(cudaEventRecord(h->group_ev[gi], s));
-    for (int k = 0; k < NC; ++k)
-      if (g.touch_mask >> k & 1u) last_touch[r][k] = gi;
     if (!hy) continue;
-    // pieces no later group reaches go down now, behind the upload
-    for (int k = 0; k < NC; ++k) {
-      if (!(g.down_mask >> k & 1u)) continue;
-      const uint64_t a = h->chunk_off[k], n = h->chunk_off[k + 1] - a;
+    for (const hostplan::Down &d : p.down) {
+      const uint64_t a = h->chunk_off[d.piece], n = h->chunk_off[d.piece + 1] - a;
       DOCI_CUDA(cudaStreamWaitEvent(cs, h->group_ev[gi], 0));
-      const int other = last_touch[1 - r][k];
-      if (other >= 0) DOCI_CUDA(cudaStreamWaitEvent(cs, h->group_ev[other], 0));
-      if (init_on[k] == 1 - r) DOCI_CUDA(cudaStreamWaitEvent(cs, h->init_ev[k], 0));
+      if (d.other_group >= 0) DOCI_CUDA(cudaStreamWaitEvent(cs, h->group_ev[d.other_group], 0));
+      if (d.wait_init) DOCI_CUDA(cudaStreamWaitEvent(cs, h->init_ev[d.piece], 0));
       if (n) DOCI_CUDA(cudaMemcpyAsync(hy + a, dy + a, n * sizeof(T), cudaMemcpyDeviceToHost, cs));
     }
   }
@@ -695,7 +548,7 @@ int launch_pair_ff_host_no(doci_ham *h, const double *hx, double *dx, double *dy
 }  // namespace
 
 int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *hy, cudaStream_t st) {
-  if (!pair_fits(h) || !h->d_pblocks_host || h->host_groups.empty()) return DOCI_ERR_INVALID;
+  if (!pair_fits(h) || !h->d_pblocks_host || h->host_steps.empty()) return DOCI_ERR_INVALID;
   int per_sm = 1;
   const int r = kernel_blocks(reinterpret_cast<const void *>(sigma_pair_kernel), kPairThreads, 0, &per_sm);
   if (r != DOCI_OK) return r;
@@ -719,7 +572,7 @@ int launch_pair_host(doci_ham *h, const float *hx, float *dx, float *dy, float *
 }
 
 int launch_pair_ff_host(doci_ham *h, const double *hx, double *dx, double *dy, double *hy, cudaStream_t st) {
-  if (!pair_ff_fits(h) || !h->d_pblocks_host || h->host_groups.empty()) return DOCI_ERR_INVALID;
+  if (!pair_ff_fits(h) || !h->d_pblocks_host || h->host_steps.empty()) return DOCI_ERR_INVALID;
   const int no = h->L - h->N + 1;
   if (no <= 8) return launch_pair_ff_host_no<8>(h, hx, dx, dy, hy, st);
   if (no <= 17) return launch_pair_ff_host_no<17>(h, hx, dx, dy, hy, st);

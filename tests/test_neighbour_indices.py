@@ -110,3 +110,39 @@ def test_tc_pair_form_ranks(tc_exe, L, N, split, us, ss):
     r = subprocess.run([tc_exe, str(L), str(N), str(split), str(us), str(ss)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad=0" in r.stdout
+
+
+PLAN_SRC = os.path.join(HERE, "host_checks", "host_plan_check.cu")
+
+
+@pytest.fixture(scope="module")
+def plan_exe(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    out = str(tmp_path_factory.mktemp("planc") / "host_plan_check")
+    subprocess.run([nvcc, "-O2", "-std=c++17", "-diag-suppress=20011", PLAN_SRC, "-o", out], check=True)
+    return out
+
+
+# the shapes' splits as the library picks them for a 152-SM GB300, plus edge shapes
+PLAN_SHAPES = [(32, 16, 16), (30, 15, 16), (28, 14, 16), (24, 12, 13), (22, 11, 11), (20, 10, 9), (18, 9, 9),
+               (26, 4, 12), (32, 2, 8), (12, 6, 8), (17, 1, 16), (9, 9, 8)]
+
+
+@pytest.mark.parametrize("L,N,split", PLAN_SHAPES)
+def test_host_schedule_orders_copies_and_groups(plan_exe, L, N, split):
+    """The host-buffer pair sigma's piece and group schedule (host_plan.h):
+    every unit in one group within its pieces, and, in a happens-before
+    simulation of the executor's three streams, each piece's upload and
+    diagonal pass before every group reaching it and all of those before the
+    piece's download."""
+    r = subprocess.run([plan_exe, str(L), str(N), str(split)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad=0" in r.stdout
+
+
+@pytest.mark.parametrize("plant", ["drop-up", "drop-other"])
+def test_host_schedule_check_catches_planted_mistakes(plan_exe, plant):
+    r = subprocess.run([plan_exe, "32", "16", "16", plant], capture_output=True, text=True)
+    assert r.returncode == 1 and "bad=0" not in r.stdout, r.stdout + r.stderr
