@@ -147,7 +147,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, long limi
   atomicCAS(err, 0, code);
   return false;
 }
-// the same wait by every lane of a warp, with one verdict for the warp (the
+// the same wait by every lane of a warp, with one outcome for the warp (the
 // .sync.aligned tensor-memory instructions that follow need the whole warp)
 __device__ __forceinline__ bool warp_wait(uint32_t a, uint32_t parity, long limit, volatile int *abort_flag, int *err,
                                           int code) {
