@@ -539,6 +539,12 @@ int launch_pair_ff_host_no(doci_ham *h, const double *hx, double *dx, double *dy
         DOCI_CUDA(cudaGetLastError());
         return static_cast<int>(DOCI_OK);
       });
+  // the side stream's groups read xf: st is ordered after them (the
+  // schedule's own join is skipped when it returns early with an error)
+  if (r != DOCI_OK && h->side_stream) {
+    cudaEventRecord(h->side_ev, h->side_stream);
+    cudaStreamWaitEvent(st, h->side_ev, 0);
+  }
   const cudaError_t ef = cudaFreeAsync(xf, st);
   if (r != DOCI_OK) return r;
   DOCI_CUDA(ef);
