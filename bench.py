@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-converge measurement")
     ap.add_argument("--converge-repeats", type=int, default=20,
                     help="mixed solves of the L=28 N=14 Hamiltonian for time-to-converge p50/p99 (0 = none)")
-    ap.add_argument("--workload", choices=["sigma", "batch", "serve", "solve", "config2"], default="sigma",
+    ap.add_argument("--workload", choices=["sigma", "batch", "serve", "solve", "l28-solvers"], default="sigma",
                     help="sigma: the headline sigma benchmark; batch: many Hamiltonians, several roots; "
                          "serve: Poisson request stream through the request server")
     ap.add_argument("--problems", type=int, default=256, help="batch: number of Hamiltonians")
@@ -501,7 +501,7 @@ def solve_workload(a):
     print(json.dumps(line), flush=True)
 
 
-def config2_workload(a):
+def l28_solvers_workload(a):
     """The plain FP64 GPU Davidson (DAVIDSON_MAX_VEC 30, DAVIDSON_KEEP 2, TOL
     1e-8, HF start) and CGP (MAX_ITS 40) on the L=28, N=14 Hamiltonian (seed
     2), wall time from a built Hamiltonian, beside the reference executable's
@@ -548,8 +548,8 @@ def main():
         return serve_workload(a)
     if a.workload == "solve":
         return solve_workload(a)
-    if a.workload == "config2":
-        return config2_workload(a)
+    if a.workload == "l28-solvers":
+        return l28_solvers_workload(a)
     import numpy as np
     import torch
     import doci_gb300 as dg

@@ -1,13 +1,13 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference itself.
 
     python tests/golden/make_golden.py --ref <reference checkout>   (or $DOCI_REFERENCE)
-    python tests/golden/make_golden.py --ref <...> --config2 [--threads T]
+    python tests/golden/make_golden.py --ref <...> --l28 [--threads T]
 
 Needs the reference checkout (its tests/ FCIDUMPs and sources) and builds
 oracle/_ref (the reference compiled from its own sources, oracle/Makefile).
 --exe only (re)makes exe/*.out: the reference executable's stdout
 (EXE_CASES below), built with and without -DDAVIDIT, run on one thread.
---config2 only (re)makes the entry "synthetic_L28_N14_s2" of golden.json:
+--l28 only (re)makes the entry "synthetic_L28_N14_s2" of golden.json:
 the reference executable's Davidson (DAVIDSON_MAX_VEC 30, DAVIDSON_KEEP 2,
 TOL 1e-8, HF start) and CGP (MAX_ITS 40) runs on the seeded L=28, N=14
 Hamiltonian (D = 40,116,600), with their iteration traces and wall times on
@@ -103,7 +103,7 @@ def exe_outputs(ref: str) -> None:
         print(name, flush=True)
 
 
-def config2(ref: str, threads: int) -> None:
+def l28_entry(ref: str, threads: int) -> None:
     """The plain FP64 Davidson and CGP of the L=28, N=14 Hamiltonian (seed 2)
     through the reference executable; merged into golden.json."""
     L, N, seed = 28, 14, 2
@@ -132,15 +132,15 @@ def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("DOCI_REFERENCE"),
                     help="reference checkout (default: $DOCI_REFERENCE)")
-    ap.add_argument("--config2", action="store_true", help="only the L=28, N=14 entry")
+    ap.add_argument("--l28", action="store_true", help="only the L=28, N=14 entry")
     ap.add_argument("--exe", action="store_true", help="only the executable's stdout fixtures")
     ap.add_argument("--threads", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
     if not a.ref:
         ap.error("give --ref or set DOCI_REFERENCE")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={a.ref}", "all", "ref"], check=True)
-    if a.config2:
-        config2(a.ref, a.threads)
+    if a.l28:
+        l28_entry(a.ref, a.threads)
         return
     if a.exe:
         exe_outputs(a.ref)

@@ -1,7 +1,7 @@
 """The plain FP64 GPU solvers on the L=28, N=14 Hamiltonian (seed 2,
 D = 40,116,600) against the reference executable's own runs of the same
 FCIDUMP (tests/golden/golden.json "synthetic_L28_N14_s2", made by
-tests/golden/make_golden.py --config2 from the reference compiled from its
+tests/golden/make_golden.py --l28 from the reference compiled from its
 sources): Davidson with DAVIDSON_MAX_VEC 30, DAVIDSON_KEEP 2, TOL 1e-8 and
 the HF start (davidson.c:33-128), and CGP with MAX_ITS 40 (CG.c:13-164),
 both dispatched as wrapper_solvers.c:15-20 does.
@@ -25,7 +25,7 @@ def dg():
     return doci_gb300
 
 
-def test_config2_davidson_fp64(synth, golden, dg):
+def test_l28_davidson_fp64(synth, golden, dg):
     g = golden["cases"][CASE]["D_exe"]
     with dg.Hamiltonian.from_fcidump(synth(28, 14, 2)) as h:
         assert h.D == golden["cases"][CASE]["D"]
@@ -39,7 +39,7 @@ def test_config2_davidson_fp64(synth, golden, dg):
         assert abs(row[1] - res) <= max(1e-3 * res, 1e-13), (it, row[1], res)
 
 
-def test_config2_cgp(synth, golden, dg):
+def test_l28_cgp(synth, golden, dg):
     g = golden["cases"][CASE]["CGP_exe"]
     with dg.Hamiltonian.from_fcidump(synth(28, 14, 2)) as h:
         r, _ = h.solve(solver="CGP", tol=1e-8, max_its=40)
