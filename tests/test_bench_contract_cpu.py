@@ -29,9 +29,9 @@ def test_reference_arm_line(tmp_path):
 
 
 def test_reference_arm_prepares_once_and_finishes(tmp_path):
-    """At the driver's default steps/warm-up the arm must end within its
-    budget: the sample (rows, diagonal) is prepared for the calibration run
-    and the sized sample only, never per step; L=20 keeps the sample cheap."""
+    """At 40 timed steps after 5 warm-ups the arm must end within its budget:
+    the sample (rows, diagonal) is prepared for the calibration run and the
+    sized sample only, never per step; L=20 keeps the sample cheap."""
     import time
     env = dict(os.environ, DOCI_BENCH_CACHE=str(tmp_path))
     t0 = time.perf_counter()
