@@ -77,6 +77,7 @@ def pair_exe(tmp_path_factory):
     (17, 1, 16, 1, 1), (17, 16, 16, 1, 1), (32, 2, 8, 1, 1), (22, 11, 11, 1, 1),
     # sampled large spaces: every visited index in range and equal to the direct rank
     (32, 16, 16, 37, 101), (28, 14, 16, 11, 31), (32, 30, 8, 3, 1), (26, 4, 12, 1, 1), (24, 12, 13, 7, 11),
+    (30, 15, 16, 29, 97), (31, 15, 16, 31, 101), (29, 14, 16, 13, 53), (27, 13, 15, 5, 23),
 ])
 def test_pair_form_ranks(pair_exe, L, N, split, bs, ss):
     r = subprocess.run([pair_exe, str(L), str(N), str(split), str(bs), str(ss)], capture_output=True, text=True)
@@ -126,8 +127,8 @@ def plan_exe(tmp_path_factory):
 
 
 # the shapes' splits as the library picks them for a 152-SM GB300, plus edge shapes
-PLAN_SHAPES = [(32, 16, 16), (30, 15, 16), (28, 14, 16), (24, 12, 13), (22, 11, 11), (20, 10, 9), (18, 9, 9),
-               (26, 4, 12), (32, 2, 8), (12, 6, 8), (17, 1, 16), (9, 9, 8)]
+PLAN_SHAPES = [(32, 16, 16), (31, 15, 16), (30, 15, 16), (29, 14, 16), (28, 14, 16), (27, 13, 15), (24, 12, 13),
+               (22, 11, 11), (20, 10, 9), (18, 9, 9), (26, 4, 12), (32, 2, 8), (12, 6, 8), (17, 1, 16), (9, 9, 8)]
 
 
 @pytest.mark.parametrize("L,N,split", PLAN_SHAPES)
